@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""Benchmark: compiled Reffine query on one GB300, against the oracle port on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1] [--impl ours|reference]
+
+A step is one run of the query over its whole synthetic table.  Default workload: the
+low-cardinality group-by (60M rows, 6 groups; config 1 of the benchmark set).  Metric: scan
+GB/s = algorithmic bytes (each referenced column read once) / time.
+
+  value      kernel throughput with the table resident in HBM (CUDA events on the launch stream)
+  e2e        the same metric through the reference-shaped host call (compile_op's function
+             pointer: ArrowTable* in, result out), host tables in pinned memory, host->device
+             copies of the referenced columns and the device->host result copy inside the timing
+  roofline   achieved algorithmic GB/s of the main kernel against the measured HBM copy peak
+  cpu_baseline  the oracle (Reffine's CPU loop restated, g++ -O3, one core) on the same table
+
+--impl reference times the oracle port alone (the reference's CPU path; it is single-threaded).
+Multi-GPU (torchrun): each rank scans its own partition (weak scaling), no collective on the
+data path; rank 0 prints the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import platform
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "scan GB/s vs HBM peak per query; batched p99 latency vs per-query launch"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduce over ranks (torch.distributed when launched by torchrun)."""
+
+    def __init__(self, world: int):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.out = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for row in csv.reader(io.StringIO(out)):
+            if len(row) < 9:
+                continue
+            try:
+                sms.append(float(row[1]))
+                maxs.append(float(row[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, row[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sms)) if sms else None, "sm_max_mhz": max(maxs) if maxs else None,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def build_workload(config: int, rank: int, world: int):
+    """Returns (name, tables list, query Func, rows, config dict).  Each rank gets its own
+    partition (a different seed), so per-GPU work is fixed as N grows."""
+    from reffine_gb300 import workloads as W
+    seed_off = 1000 * rank
+    if config == 0:
+        n = 6_000_000
+        t = W.filter_sum_table(n, seed=0 + seed_off)
+        return ("filter_sum_6M", [t], W.filter_sum_query(t.get_data_type()), n,
+                {"rows": n, "query": "SUM(price*discount), COUNT over day in [730,1095), discount in [0.05,0.07], "
+                                     "quantity < 24"})
+    if config == 1:
+        n = 60_000_000
+        t = W.groupby_table(n, seed=1 + seed_off)
+        return ("groupby_6groups_60M", [t], W.groupby_query(t.get_data_type()), n,
+                {"rows": n, "groups": 6, "query": "per (flag_a, flag_b): SUM qty/price/disc_price/charge, AVG "
+                                                  "qty/price/disc, COUNT over day <= 2450"})
+    if config == 3:
+        nb, npr = 10_000_000, 200_000_000
+        b, p = W.join_tables(nb, npr, seed=3 + seed_off)
+        return ("join_10M_x_200M", [b, p], W.join_query(b.get_data_type(), p.get_data_type()), npr,
+                {"rows": npr, "build_rows": nb, "query": "SUM(amount), COUNT per build attr < 5, probe day in [0,365)"})
+    raise SystemExit("config %d is not benchmarked by this script" % config)
+
+
+def referenced_bytes(plan, tables) -> int:
+    from reffine_gb300.ir import DataType
+    tot = 0
+    for i, t in enumerate(tables):
+        tot += int(plan.info.bytes_per_row[i]) * len(t)
+    return tot
+
+
+def cpu_baseline(fn, tables, nbytes, budget_s=20.0):
+    """The oracle port (serial C++ loop, one core) on the same tables."""
+    from oracle import loopgen
+    q = loopgen.Query(fn)
+    out, cargs = q.prepare(*tables)
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < 5 and (not times or time.perf_counter() + times[-1] < t_end):
+        t0 = time.perf_counter()
+        q.run_prepared(out, cargs)
+        times.append(time.perf_counter() - t0)
+    sec = float(np.median(times))
+    return {"value": nbytes / sec / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+            "sample": "the full table, %d run(s), median %.3f s; %s" % (len(times), sec, platform.processor() or
+                                                                        platform.machine())}, sec
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    name, tables, fn, rows, cfg = build_workload(args.config, 0, 1)
+    from reffine_gb300 import engine
+    # algorithmic bytes come from the lowering's column analysis (no GPU needed for it)
+    from oracle import loopgen
+    nbytes = sum(t.nbytes(_cols_read_cpu(fn, i)) for i, t in enumerate(tables))
+    q = loopgen.Query(fn)
+    out, cargs = q.prepare(*tables)
+    for _ in range(args.warmup):
+        q.run_prepared(out, cargs)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        q.run_prepared(out, cargs)
+        times.append(time.perf_counter() - t0)
+    sec = float(np.mean(times))
+    val = nbytes / sec / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": name, **cfg, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": val, "unit": "GB/s", "cores": 1, "kind": "port",
+                             "sample": "the full table per step (Reffine's serial loop restated, g++ -O3)"},
+            "e2e": {"value": val, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _cols_read_cpu(fn, input_idx):
+    """Referenced columns of a Func input, from the lowering (rf_plan_check's source)."""
+    import re
+    from reffine_gb300 import engine
+    src = engine.check(fn)
+    slot = 0
+    for i, s in enumerate(fn.inputs):
+        if i == input_idx:
+            break
+        if s.type.is_vector():
+            slot += 1
+    return sorted({int(c) for c in re.findall(r"P\.t\[%d\]\.col\[(\d+)\]" % slot, src)})
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    from reffine_gb300 import cudart, engine
+    dist = Dist(world)
+    eng = engine.Engine(local)
+    name, tables, fn, rows, cfg = build_workload(args.config, rank, world)
+    dts = [eng.upload(t) for t in tables]
+    plan = eng.compile(fn)
+    nbytes = referenced_bytes(plan, tables)
+    pargs = plan.args(*dts)
+    n = len(dts)
+    stream = eng.stream
+    out_check = plan.new_out()
+
+    for _ in range(max(args.warmup, 3)):
+        plan.launch(pargs, n)
+    eng.sync()
+
+    evs = [cudart.Event() for _ in range(args.steps + 1)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    eng.sync()
+    l0 = eng.launch_count()
+    evs[0].record(stream)
+    for k in range(args.steps):
+        plan.launch(pargs, n)
+        evs[k + 1].record(stream)
+    eng.sync()
+    dist.barrier()
+    l1 = eng.launch_count()
+    clk = clocks.stop()
+    per = [evs[k].elapsed_ms(evs[k + 1]) for k in range(args.steps)]
+    total_ms = dist.max(sum(per))
+    ms_step = total_ms / args.steps
+    all_bytes = dist.sum(nbytes)
+    value = all_bytes / (ms_step / 1e3) / 1e9
+    plan.run_args(pargs, n, out_check)  # result of the last configuration, for the log
+
+    # kernel roofline (this rank): algorithmic bytes per launch / mean launch time
+    peak, peak_kind = peak_hbm()
+    kern_ms = float(np.mean(per))
+    achieved = nbytes / (kern_ms / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(name)
+        except Exception:
+            traffic = None
+
+    # end to end through the reference-shaped call: host tables in pinned memory
+    e2e = None
+    h2d = sum(int(plan.info.bytes_per_row[i]) * len(t) for i, t in enumerate(tables))
+    try:
+        from reffine_gb300.table import Column, Table
+        pinned = []
+        ptables = []
+        for t in tables:
+            cols = []
+            for c in t.columns:
+                buf = eng.host_alloc(c.data.nbytes)
+                v = buf.view(c.data.dtype, len(c.data))
+                v[:] = c.data
+                pinned.append(buf)
+                cols.append(Column(c.name, c.dtype, v, c.valid, c.run_ends))
+            ptables.append(Table(t.name, t.dim, cols))
+        q = engine.compile_op(fn, engine=eng)
+        q(*ptables)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            q(*ptables)
+        e2e_s = dist.max(time.perf_counter() - t0) / args.e2e_steps
+        e2e = {"value": all_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": int(plan.info.output_size), "ms_per_step": e2e_s * 1e3,
+               "path": "compile_op function pointer (rf_plan_thunk), pinned host tables"}
+        del ptables
+        for b in pinned:
+            b.free()
+    except Exception as ex:  # report, do not hide
+        e2e = {"value": None, "unit": "GB/s", "error": str(ex)[:300], "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": int(plan.info.output_size)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu, _ = cpu_baseline(fn, tables, nbytes)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": name, **cfg, "bytes_per_step": nbytes, "l2": "inputs larger than L2 (no flush)"},
+                "rows_per_s": rows * world / (ms_step / 1e3),
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                             "kernel": "rf_main (%s)" % ("grouped scan-reduce" if plan.kind == 2 else "scan-reduce"),
+                             "algorithmic_bytes_per_launch": nbytes},
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(l1 - l0), "clocks": clk,
+                "result_sample": str(engine.from_c(out_check))[:200]}
+        print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,180 @@
+// Device-side building blocks of every query kernel (GB300, sm_103a).
+//
+// A query's kernels are compiled at plan time: the lowering pass (lower.cpp) emits a short
+// source that defines the query's fragment - its row function, accumulator type, group
+// function and epilogue - and then instantiates one of the templates below.  This header is
+// handed to NVRTC as an in-memory header; it includes nothing from the system.
+//
+// Row-access helpers restate Reffine's runtime helpers (include/reffine/vinstr/vinstr.h):
+//   rf_valid   get_null_bit  (vinstr.h:70-74): bitmap read as uint16 words; NULL = all valid
+//   rf_runend  read_runend_buf (vinstr.h:15-23): int32 run ends, 0 for index < 0
+//   rf_locate  vector_locate (vinstr.h:137-146): hash-index probe, -1 on a miss
+//   rf_rd      a Load of get_array_buf(...)[idx] (readwritepass.cpp:16-30), guarded: an index
+//              outside the column reads 0 (the reference reads out of bounds there)
+#pragma once
+
+#ifdef __CUDACC_RTC__
+typedef signed char int8_t;
+typedef short int16_t;
+typedef int int32_t;
+typedef long long int64_t;
+typedef unsigned char uint8_t;
+typedef unsigned short uint16_t;
+typedef unsigned int uint32_t;
+typedef unsigned long long uint64_t;
+#define RF_INT64_MAX 0x7fffffffffffffffLL
+#else
+#include <cstdint>
+#define RF_INT64_MAX 0x7fffffffffffffffLL
+#endif
+
+#include "rf_params.h"
+
+#define RF_DEV static __device__ __forceinline__
+
+// ---------------------------------------------------------------------------------------
+// column loads: read-only path (ld.global.nc), values are read once per query
+// ---------------------------------------------------------------------------------------
+template <class T>
+struct RfLd;
+template <>
+struct RfLd<bool> {
+    RF_DEV bool ld(const void* p, long long i) { return __ldg((const signed char*)p + i) != 0; }
+};
+template <>
+struct RfLd<int8_t> {
+    RF_DEV int8_t ld(const void* p, long long i) { return __ldg((const signed char*)p + i); }
+};
+template <>
+struct RfLd<uint8_t> {
+    RF_DEV uint8_t ld(const void* p, long long i) { return __ldg((const unsigned char*)p + i); }
+};
+template <>
+struct RfLd<int16_t> {
+    RF_DEV int16_t ld(const void* p, long long i) { return __ldg((const short*)p + i); }
+};
+template <>
+struct RfLd<uint16_t> {
+    RF_DEV uint16_t ld(const void* p, long long i) { return __ldg((const unsigned short*)p + i); }
+};
+template <>
+struct RfLd<int32_t> {
+    RF_DEV int32_t ld(const void* p, long long i) { return __ldg((const int*)p + i); }
+};
+template <>
+struct RfLd<uint32_t> {
+    RF_DEV uint32_t ld(const void* p, long long i) { return __ldg((const unsigned int*)p + i); }
+};
+template <>
+struct RfLd<int64_t> {
+    RF_DEV int64_t ld(const void* p, long long i) { return __ldg((const long long*)p + i); }
+};
+template <>
+struct RfLd<uint64_t> {
+    RF_DEV uint64_t ld(const void* p, long long i) { return __ldg((const unsigned long long*)p + i); }
+};
+template <>
+struct RfLd<float> {
+    RF_DEV float ld(const void* p, long long i) { return __ldg((const float*)p + i); }
+};
+template <>
+struct RfLd<double> {
+    RF_DEV double ld(const void* p, long long i) { return __ldg((const double*)p + i); }
+};
+
+template <class T>
+RF_DEV T rf_ld(const void* p, long long i)
+{
+    return RfLd<T>::ld(p, i);
+}
+
+// guarded read of column `c` at row/run `i`
+template <class T>
+RF_DEV T rf_rd(const RfCol& c, long long i)
+{
+    return (i >= 0 && i < c.len) ? rf_ld<T>(c.data, i) : T(0);
+}
+
+RF_DEV bool rf_valid(const unsigned short* bm, long long i)
+{
+    return !bm || ((__ldg(bm + (i >> 4)) >> (i & 15)) & 1u);
+}
+
+RF_DEV long long rf_runend(const RfCol& c, long long i)
+{
+    return i < 0 ? 0LL : (long long)__ldg(c.run_ends + i);
+}
+
+// std::max / std::min semantics (what the reference's emitted C++ calls)
+template <class T>
+RF_DEV T rf_max(T a, T b)
+{
+    return (a < b) ? b : a;
+}
+template <class T>
+RF_DEV T rf_min(T a, T b)
+{
+    return (b < a) ? b : a;
+}
+
+// ---------------------------------------------------------------------------------------
+// hash index probe
+// ---------------------------------------------------------------------------------------
+// 64-bit finaliser of MurmurHash3 (Austin Appleby, public domain): a bijective mixer, so
+// distinct keys never collide before range reduction.
+RF_DEV unsigned long long rf_mix64(unsigned long long x)
+{
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return x;
+}
+
+// slot of a key in a table of `cap` slots: multiply-high range reduction of the mixed key
+RF_DEV unsigned long long rf_home(long long key, unsigned long long cap)
+{
+    return __umul64hi(rf_mix64((unsigned long long)key), cap);
+}
+
+RF_DEV long long rf_locate(const RfIndex& ix, long long key)
+{
+    if (ix.cap == 0) return -1;
+    if (key == RF_EMPTY_KEY) {
+        long long r = *ix.special;
+        return r == RF_INT64_MAX ? -1 : r;
+    }
+    unsigned long long h = rf_home(key, ix.cap);
+    const longlong2* s = (const longlong2*)ix.slots;
+    for (unsigned long long n = 0; n < ix.cap; ++n) {
+        longlong2 v = __ldg(s + h);
+        if (v.x == key) return v.y;
+        if (v.x == RF_EMPTY_KEY) return -1;
+        if (++h == ix.cap) h = 0;
+    }
+    return -1;
+}
+
+RF_DEV void rf_set_err(const RfParams& P, int code)
+{
+    if (P.err) atomicCAS(P.err, 0, code);
+}
+
+// 8-byte words through L2 (coherent between the blocks of one grid)
+RF_DEV void rf_st_words(void* dst, const void* src, int nbytes)
+{
+    unsigned long long* d = (unsigned long long*)dst;
+    const unsigned long long* s = (const unsigned long long*)src;
+    for (int i = 0; i < nbytes / 8; i++) __stcg(d + i, s[i]);
+}
+RF_DEV void rf_ld_words(void* dst, const void* src, int nbytes)
+{
+    unsigned long long* d = (unsigned long long*)dst;
+    const unsigned long long* s = (const unsigned long long*)src;
+    for (int i = 0; i < nbytes / 8; i++) d[i] = __ldcg(s + i);
+}
+
+// 64-bit slot encodings
+RF_DEV unsigned long long rf_f2u(double x) { return (unsigned long long)__double_as_longlong(x); }
+RF_DEV double rf_u2f(unsigned long long x) { return __longlong_as_double((long long)x); }

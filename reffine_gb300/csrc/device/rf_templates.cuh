@@ -1,0 +1,167 @@
+// Kernel templates of the GB300 backend.  Included by a generated query source AFTER the
+// query's fragment (the templates use the fragment's types and functions), once per source.
+#pragma once
+
+// ---------------------------------------------------------------------------------------
+// Template 1: fused scan-filter-project-reduce.
+//   The fragment defines: struct RfAcc (8-byte aligned fields, size a multiple of 8),
+//   rf_acc_init(P, A), rf_acc_combine(A, B) (A <- A op B), rf_acc_shfl(A, off),
+//   rf_row(P, r, A) (one row) and rf_finish(P, A, out).
+// Work is split into fixed tiles of P.tile_rows rows; unit u takes tiles u, u+nunits, ...
+// Each unit's accumulator goes to P.partials[u]; the last unit to finish folds the partials in
+// a fixed order.  So the result depends only on (rows, tile_rows, nunits, threads), not on
+// scheduling: a query gives the same bits alone or batched with others.
+// ---------------------------------------------------------------------------------------
+#ifdef RF_SCAN_REDUCE
+template <int T>
+RF_DEV void rf_scan_reduce_rows(const RfParams& P, int unit, int nunits, RfAcc& acc)
+{
+    long long lo = P.row_lo, hi = P.row_hi;
+    if (P.range) {
+        long long b = P.range[0], e = P.range[1];
+        lo = b > lo ? b : lo;
+        hi = e < hi ? e : hi;
+    }
+    const long long tr = P.tile_rows;
+    const long long ntiles = (P.row_hi - P.row_lo + tr - 1) / tr;
+    for (long long tile = unit; tile < ntiles; tile += nunits) {
+        long long r0 = P.row_lo + tile * tr, r1 = r0 + tr;
+        if (r1 > hi) r1 = hi;
+        if (r0 < lo) r0 = lo;
+#pragma unroll 4
+        for (long long r = r0 + threadIdx.x; r < r1; r += T) rf_row(P, r, acc);
+    }
+}
+
+template <int T>
+RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc& acc)
+{
+    __shared__ RfAcc warp_acc[T / 32];
+    __shared__ int last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        RfAcc o = rf_acc_shfl(acc, off);
+        rf_acc_combine(acc, o);
+    }
+    if (lane == 0) warp_acc[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        RfAcc tot = warp_acc[0];
+        for (int w = 1; w < T / 32; w++) rf_acc_combine(tot, warp_acc[w]);
+        rf_st_words((RfAcc*)P.partials + unit, &tot, (int)sizeof(RfAcc));
+        __threadfence();
+        unsigned int ticket = atomicAdd(P.counter, 1u);
+        last = (ticket == (unsigned int)nunits - 1u);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (warp == 0) {
+        RfAcc tot;
+        rf_acc_init(P, tot);
+        for (int u = lane; u < nunits; u += 32) {
+            RfAcc p;
+            rf_ld_words(&p, (const RfAcc*)P.partials + u, (int)sizeof(RfAcc));
+            rf_acc_combine(tot, p);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            RfAcc o = rf_acc_shfl(tot, off);
+            rf_acc_combine(tot, o);
+        }
+        if (lane == 0) {
+            rf_finish(P, tot, P.out);
+            *P.counter = 0u;
+        }
+    }
+}
+
+#define RF_SCAN_REDUCE_KERNEL(NAME, T)                                                      \
+    extern "C" __global__ void __launch_bounds__(T) NAME(const __grid_constant__ RfParams P) \
+    {                                                                                       \
+        RfAcc acc;                                                                          \
+        rf_acc_init(P, acc);                                                                \
+        rf_scan_reduce_rows<T>(P, blockIdx.x, gridDim.x, acc);                              \
+        rf_scan_reduce_merge<T>(P, blockIdx.x, gridDim.x, acc);                             \
+    }
+#endif  // RF_SCAN_REDUCE
+
+// ---------------------------------------------------------------------------------------
+// Template 2: grouped scan-reduce with shared-memory privatised accumulators.
+//   The fragment defines RF_G groups x RF_M aggregates, struct RfVals, rf_group(P, r, V)
+//   (group id or -1, and the row's aggregate inputs), rf_slot_init(m) (64-bit identity),
+//   rf_slot_combine(m, a, b), rf_slot_add(S, g, t, V) and rf_finish_groups(P, tot, out).
+// Each thread owns a private column of G*M 64-bit slots in shared memory (slot (q, t) at
+// S[q * T + t]): no atomics and no bank conflicts on the per-row update.  At the end every
+// slot column is folded over the block in a fixed order, then over units by the last unit.
+// ---------------------------------------------------------------------------------------
+#ifdef RF_GROUP_REDUCE
+template <int T>
+RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
+{
+    extern __shared__ unsigned long long S[];
+    __shared__ int last;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int Q = RF_G * RF_M;
+    for (int q = 0; q < Q; q++) S[q * T + tid] = rf_slot_init(P, q % RF_M);
+    long long lo = P.row_lo, hi = P.row_hi;
+    if (P.range) {
+        long long b = P.range[0], e = P.range[1];
+        lo = b > lo ? b : lo;
+        hi = e < hi ? e : hi;
+    }
+    const long long tr = P.tile_rows;
+    const long long ntiles = (P.row_hi - P.row_lo + tr - 1) / tr;
+    for (long long tile = unit; tile < ntiles; tile += nunits) {
+        long long r0 = P.row_lo + tile * tr, r1 = r0 + tr;
+        if (r1 > hi) r1 = hi;
+        if (r0 < lo) r0 = lo;
+#pragma unroll 4
+        for (long long r = r0 + tid; r < r1; r += T) {
+            RfVals V;
+            int g = rf_group(P, r, V);
+            if (g >= 0) rf_slot_add(S, g, tid, V);
+        }
+    }
+    __syncthreads();
+    unsigned long long* part = (unsigned long long*)P.partials;
+    for (int q = warp; q < Q; q += T / 32) {
+        const int m = q % RF_M;
+        unsigned long long a = S[q * T + lane];
+        for (int k = 1; k < T / 32; k++) a = rf_slot_combine(m, a, S[q * T + lane + 32 * k]);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) a = rf_slot_combine(m, a, __shfl_down_sync(0xffffffffu, a, off));
+        if (lane == 0) __stcg(part + (long long)unit * Q + q, a);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        unsigned int ticket = atomicAdd(P.counter, 1u);
+        last = (ticket == (unsigned int)nunits - 1u);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int q = warp; q < Q; q += T / 32) {
+        const int m = q % RF_M;
+        unsigned long long a = rf_slot_init(P, m);
+        for (int u = lane; u < nunits; u += 32) a = rf_slot_combine(m, a, __ldcg(part + (long long)u * Q + q));
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) a = rf_slot_combine(m, a, __shfl_down_sync(0xffffffffu, a, off));
+        if (lane == 0) S[q] = a;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        rf_finish_groups(P, S, P.out);
+        *P.counter = 0u;
+    }
+}
+
+#define RF_GROUP_REDUCE_KERNEL(NAME, T)                                                     \
+    extern "C" __global__ void __launch_bounds__(T) NAME(const __grid_constant__ RfParams P) \
+    {                                                                                       \
+        rf_group_reduce<T>(P, blockIdx.x, gridDim.x);                                       \
+    }
+#endif  // RF_GROUP_REDUCE
+

@@ -1,0 +1,77 @@
+// Query-independent device kernels, compiled ahead of time with nvcc for sm_103a.
+//
+//   rf_index_*   the device hash index of a table's iterator column: the GPU form of
+//                ArrowTable2::build_index (include/reffine/arrow/table.h:107-138), an
+//                std::unordered_map<int64, row> built serially there.  Here: open addressing,
+//                linear probing, load factor 0.5, {key, row} slots of 16 bytes (one load per
+//                probe); the lowest row of a duplicated key wins (emplace keeps the first).
+#include <cuda_runtime.h>
+
+#include "device/rf_device.cuh"
+#include "kernels.h"
+
+namespace {
+
+__global__ void index_init_kernel(long long* slots, unsigned long long cap, long long* special)
+{
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (; i < cap; i += stride) {
+        longlong2 v;
+        v.x = RF_EMPTY_KEY;
+        v.y = RF_INT64_MAX;
+        reinterpret_cast<longlong2*>(slots)[i] = v;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *special = RF_INT64_MAX;
+}
+
+// keys: int64 column 0 (run values for a run-end column), n entries, validity bitmap or NULL
+__global__ void index_build_kernel(const long long* __restrict__ keys, const unsigned short* __restrict__ valid,
+                                   long long n, long long* slots, unsigned long long cap, long long* special,
+                                   int* err)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) {
+        if (!rf_valid(valid, i)) continue;
+        long long k = __ldg(keys + i);
+        if (k == RF_EMPTY_KEY) {
+            atomicMin(special, i);
+            continue;
+        }
+        unsigned long long h = rf_home(k, cap);
+        bool done = false;
+        // bounded: at most `cap` probes (the table is half empty, so a few in practice)
+        for (unsigned long long p = 0; p < cap; ++p) {
+            unsigned long long* kp = reinterpret_cast<unsigned long long*>(slots + 2 * h);
+            unsigned long long old = atomicCAS(kp, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)k);
+            if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)k) {
+                atomicMin(slots + 2 * h + 1, i);
+                done = true;
+                break;
+            }
+            if (++h == cap) h = 0;
+        }
+        if (!done && err) atomicCAS(err, 0, RF_DEVERR_PROBE);
+    }
+}
+
+int grid_for(long long n, int threads)
+{
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 152 * 16) b = 152 * 16;
+    return (int)b;
+}
+
+}  // namespace
+
+extern "C" int rf_k_index_build(const void* keys, const unsigned short* valid, long long n, long long* slots,
+                                unsigned long long cap, long long* special, int* err, cudaStream_t stream)
+{
+    index_init_kernel<<<grid_for((long long)cap, 256), 256, 0, stream>>>(slots, cap, special);
+    if (n > 0)
+        index_build_kernel<<<grid_for(n, 256), 256, 0, stream>>>(static_cast<const long long*>(keys), valid, n, slots,
+                                                                 cap, special, err);
+    return (int)cudaGetLastError();
+}

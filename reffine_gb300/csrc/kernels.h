@@ -1,0 +1,16 @@
+// Host launchers of the ahead-of-time kernels in kernels.cu.
+#pragma once
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Builds the device hash index of an int64 key column (2 launches).  Returns a cudaError_t.
+int rf_k_index_build(const void* keys, const unsigned short* valid, long long n, long long* slots,
+                     unsigned long long cap, long long* special, int* err, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,1637 @@
+// Lowering pass: Reffine Func -> kernel template + device fragment (CUDA source).
+//
+// Reference semantics restated here (Reffine, file:line):
+//   iteration spaces   src/pass/reffinepass.cpp:55-123, src/iter/iter_space.cpp (VecSpace,
+//                      LBound/UBound/Filtered, the & composition at :6-12)
+//   Reduce             src/pass/loopgen.cpp:206-269: row loop over a SubVector (condition:
+//                      validity of column 1) or over an Op's iteration space; the accumulator
+//                      is applied in row order
+//   struct state       src/pass/scalarpass.cpp:121-137 (field-by-field stores)
+//   constants          src/pass/cemitter.cpp:89-107 (FP constants printed with 6 decimals)
+//   expressions        src/pass/cemitter.cpp:112-160 (C++ operators and std::max/std::min)
+#include "lower.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <set>
+#include <sstream>
+
+namespace rfg {
+
+using namespace reffine;
+
+namespace {
+
+// ------------------------------------------------------------------------------------------
+// IR utilities
+// ------------------------------------------------------------------------------------------
+template <class T>
+const T* as(const Expr& e)
+{
+    return static_cast<const T*>(e.get());
+}
+
+bool is_kind(const Expr& e, NodeKind k) { return e && e->kind == k; }
+
+bool is_nary(const Expr& e, MathOp op) { return is_kind(e, NodeKind::NARY) && as<NaryExpr>(e)->op == op; }
+
+// structural equality (symbols by identity)
+bool same(const Expr& a, const Expr& b)
+{
+    if (a.get() == b.get()) return true;
+    if (!a || !b || a->kind != b->kind || a->type != b->type) return false;
+    switch (a->kind) {
+        case NodeKind::SYM: return false;
+        case NodeKind::CONST: return as<Const>(a)->val == as<Const>(b)->val;
+        case NodeKind::NARY: {
+            auto x = as<NaryExpr>(a), y = as<NaryExpr>(b);
+            if (x->op != y->op || x->args.size() != y->args.size()) return false;
+            for (size_t i = 0; i < x->args.size(); i++)
+                if (!same(x->args[i], y->args[i])) return false;
+            return true;
+        }
+        case NodeKind::SELECT: {
+            auto x = as<Select>(a), y = as<Select>(b);
+            return same(x->cond, y->cond) && same(x->true_body, y->true_body) && same(x->false_body, y->false_body);
+        }
+        case NodeKind::CAST: return same(as<Cast>(a)->arg, as<Cast>(b)->arg);
+        case NodeKind::GET: return as<Get>(a)->col == as<Get>(b)->col && same(as<Get>(a)->val, as<Get>(b)->val);
+        case NodeKind::NEW: {
+            auto x = as<New>(a), y = as<New>(b);
+            if (x->vals.size() != y->vals.size()) return false;
+            for (size_t i = 0; i < x->vals.size(); i++)
+                if (!same(x->vals[i], y->vals[i])) return false;
+            return true;
+        }
+        case NodeKind::ELEMENT: return same(as<Element>(a)->vec, as<Element>(b)->vec) && same(as<Element>(a)->iter, as<Element>(b)->iter);
+        case NodeKind::LENGTH: return as<Length>(a)->col == as<Length>(b)->col && same(as<Length>(a)->vec, as<Length>(b)->vec);
+        case NodeKind::LOCATE: return same(as<Locate>(a)->vec, as<Locate>(b)->vec) && same(as<Locate>(a)->iter, as<Locate>(b)->iter);
+        case NodeKind::READDATA:
+            return as<ReadData>(a)->col == as<ReadData>(b)->col && same(as<ReadData>(a)->vec, as<ReadData>(b)->vec) &&
+                   same(as<ReadData>(a)->idx, as<ReadData>(b)->idx);
+        default: return false;
+    }
+}
+
+void children(const Expr& e, std::vector<Expr>& out)
+{
+    switch (e->kind) {
+        case NodeKind::NARY: for (auto& a : as<NaryExpr>(e)->args) out.push_back(a); break;
+        case NodeKind::SELECT: {
+            auto s = as<Select>(e);
+            out.push_back(s->cond), out.push_back(s->true_body), out.push_back(s->false_body);
+            break;
+        }
+        case NodeKind::CAST: out.push_back(as<Cast>(e)->arg); break;
+        case NodeKind::GET: out.push_back(as<Get>(e)->val); break;
+        case NodeKind::NEW: for (auto& v : as<New>(e)->vals) out.push_back(v); break;
+        case NodeKind::OP: {
+            auto o = as<Op>(e);
+            for (auto& i : o->iters) out.push_back(i);
+            out.push_back(o->pred);
+            for (auto& x : o->outputs) out.push_back(x);
+            break;
+        }
+        case NodeKind::ELEMENT: out.push_back(as<Element>(e)->vec), out.push_back(as<Element>(e)->iter); break;
+        case NodeKind::IN: out.push_back(as<In>(e)->iter), out.push_back(as<In>(e)->vec); break;
+        case NodeKind::REDUCE: {
+            auto r = as<Reduce>(e);
+            out.push_back(r->vec), out.push_back(r->init_expr), out.push_back(r->acc_expr);
+            break;
+        }
+        case NodeKind::SUBVECTOR: {
+            auto s = as<SubVector>(e);
+            out.push_back(s->vec), out.push_back(s->start), out.push_back(s->end);
+            break;
+        }
+        case NodeKind::LENGTH: out.push_back(as<Length>(e)->vec); break;
+        case NodeKind::LOCATE: out.push_back(as<Locate>(e)->vec), out.push_back(as<Locate>(e)->iter); break;
+        case NodeKind::READDATA: out.push_back(as<ReadData>(e)->vec), out.push_back(as<ReadData>(e)->idx); break;
+        default: break;
+    }
+}
+
+// does `e` (following table symbols through `tbl`) reference a node in `targets`?
+bool mentions(const Expr& e, const std::set<const ExprNode*>& targets, const SymTable& tbl,
+              std::set<const ExprNode*>& seen)
+{
+    if (!e) return false;
+    if (targets.count(e.get())) return true;
+    if (seen.count(e.get())) return false;
+    seen.insert(e.get());
+    if (e->kind == NodeKind::SYM) {
+        auto it = tbl.find(std::static_pointer_cast<SymNode>(e));
+        return it != tbl.end() && mentions(it->second, targets, tbl, seen);
+    }
+    std::vector<Expr> ch;
+    children(e, ch);
+    for (auto& c : ch)
+        if (mentions(c, targets, tbl, seen)) return true;
+    return false;
+}
+
+bool mentions(const Expr& e, const ExprNode* target, const SymTable& tbl)
+{
+    std::set<const ExprNode*> t{target}, seen;
+    return mentions(e, t, tbl, seen);
+}
+
+void flatten_and(const Expr& e, std::vector<Expr>& out)
+{
+    if (is_nary(e, MathOp::AND)) {
+        flatten_and(as<NaryExpr>(e)->args[0], out);
+        flatten_and(as<NaryExpr>(e)->args[1], out);
+    } else {
+        out.push_back(e);
+    }
+}
+
+std::string hexkey(const std::string& s)
+{
+    // FNV-1a 64 over the source: a stable cache key
+    unsigned long long h = 1469598103934665603ULL;
+    for (unsigned char c : s) h = (h ^ c) * 1099511628211ULL;
+    char b[32];
+    snprintf(b, sizeof b, "%016llx", h);
+    return b;
+}
+
+std::string ctype(const DataType& t)
+{
+    switch (t.btype) {
+        case BOOL: return "bool";
+        case INT8: return "int8_t";
+        case UINT8: return "uint8_t";
+        case INT16: return "int16_t";
+        case UINT16: return "uint16_t";
+        case INT32: return "int32_t";
+        case UINT32: return "uint32_t";
+        case INT64: case IDX: return "int64_t";
+        case UINT64: return "uint64_t";
+        case FLOAT32: return "float";
+        case FLOAT64: return "double";
+        default: throw LowerError("no device type for " + t.str());
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Values produced by the expression emitter
+// ------------------------------------------------------------------------------------------
+struct Val {
+    enum K { SCALAR, STRUCT, VEC, SUBVEC } k = SCALAR;
+    std::string c;
+    std::vector<Val> f;
+    int slot = -1;
+    int input = -1;
+    const ExprNode* vnode = nullptr;
+    std::string s, e;
+    DataType type;
+};
+
+// ------------------------------------------------------------------------------------------
+// Accumulator leaves of a Reduce state
+// ------------------------------------------------------------------------------------------
+enum class AggOp { NONE, SUM, MIN, MAX, OR, AND };
+
+struct Leaf {
+    std::vector<size_t> path;
+    DataType type;
+    AggOp op = AggOp::NONE;
+    Expr cond;               // null = every row
+    Expr value;              // the row's contribution
+    bool state_first = true; // std::max(s, e) vs std::max(e, s)
+    bool count = false;      // value is the constant 1: accumulate as an integer count
+    Expr init;
+    // grouping
+    std::vector<Expr> filters;
+    std::vector<std::pair<Expr, Expr>> keys;  // (key expression, constant)
+};
+
+const char* agg_name(AggOp op)
+{
+    switch (op) {
+        case AggOp::SUM: return "sum";
+        case AggOp::MIN: return "min";
+        case AggOp::MAX: return "max";
+        case AggOp::OR: return "or";
+        case AggOp::AND: return "and";
+        default: return "none";
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Iteration space of a single-iterator Op (reffinepass.cpp:55-105 composed by & as in
+// iter_space.cpp:6-12): base VecSpace or UniversalSpace, wrapped by LBound/UBound/Filtered.
+// ------------------------------------------------------------------------------------------
+struct Space {
+    bool has_vec = false;
+    int vec_input = -1;              // Func input of the iterated vector
+    Expr vec_node;                   // the vector expression (In's vec)
+    Expr iter;                       // the iterator symbol
+    std::vector<Expr> lbs, ubs;      // bound expressions (iter >= lb, iter <= ub)
+    std::vector<Expr> filters;       // boolean symbols
+    int n_vecs = 0;
+};
+
+class Lowerer {
+public:
+    Lowerer(std::shared_ptr<Func> fn, bool vectorize) : fn_(std::move(fn)), vectorize_(vectorize) {}
+
+    Plan run()
+    {
+        plan_.vectorize = vectorize_;
+        plan_.n_inputs = (int)fn_->inputs.size();
+        int tslot = 0, sslot = 0;
+        for (size_t i = 0; i < fn_->inputs.size(); i++) {
+            auto& s = fn_->inputs[i];
+            plan_.input_types.push_back(s->type);
+            plan_.cols_read.emplace_back();
+            plan_.needs_index.push_back(0);
+            if (s->type.is_vector()) {
+                if (tslot >= RF_MAX_TABLES_) throw LowerError("too many table inputs");
+                if (s->type.dtypes.size() > (size_t)RF_MAX_COLS_) throw LowerError("too many columns");
+                plan_.table_slot.push_back(tslot++);
+                plan_.scalar_slot.push_back(-1);
+            } else if (s->type.is_primitive()) {
+                if (sslot >= RF_MAX_SCALARS_) throw LowerError("too many scalar inputs");
+                plan_.table_slot.push_back(-1);
+                plan_.scalar_slot.push_back(sslot++);
+            } else {
+                throw LowerError("struct inputs are not supported", false);  // scalarpass.cpp:201-203
+            }
+            input_index_[s.get()] = (int)i;
+        }
+        plan_.out_type = fn_->output->type;
+        Expr root = resolve(fn_->output);
+        if (root->type.is_vector()) {
+            if (root->kind != NodeKind::OP) throw LowerError("a vector output must be an Op");
+            lower_op(root);
+        } else {
+            std::vector<const Reduce*> reds;
+            find_reduces(fn_->output, reds);
+            if (reds.size() != 1) throw LowerError("the GPU backend lowers Funcs with exactly one Reduce");
+            lower_reduce(*reds[0]);
+        }
+        plan_.key = hexkey(plan_.source);
+        return plan_;
+    }
+
+private:
+    static constexpr int RF_MAX_TABLES_ = 4, RF_MAX_COLS_ = 24, RF_MAX_SCALARS_ = 16, RF_MAX_CONSTS_ = 128;
+
+    // follow a symbol to its table entry (top-level structure only)
+    Expr resolve(const Expr& e) const
+    {
+        Expr x = e;
+        for (int n = 0; n < 64 && x->kind == NodeKind::SYM; n++) {
+            auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(x));
+            if (it == fn_->tbl.end()) break;
+            x = it->second;
+        }
+        return x;
+    }
+
+    void find_reduces(const Expr& e, std::vector<const Reduce*>& out)
+    {
+        std::set<const ExprNode*> seen;
+        std::function<void(const Expr&)> rec = [&](const Expr& x) {
+            if (!x || seen.count(x.get())) return;
+            seen.insert(x.get());
+            if (x->kind == NodeKind::REDUCE) {
+                out.push_back(as<Reduce>(x));
+                return;
+            }
+            if (x->kind == NodeKind::SYM) {
+                auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(x));
+                if (it != fn_->tbl.end()) rec(it->second);
+                return;
+            }
+            std::vector<Expr> ch;
+            children(x, ch);
+            for (auto& c : ch) rec(c);
+        };
+        rec(e);
+    }
+
+    // ---------------------------------------------------------------- constants & inputs
+    std::string konst(const Const& c)
+    {
+        if (c.type.btype == BOOL) return c.val != 0 ? "true" : "false";
+        ConstSlot k;
+        if (c.type.is_float()) {
+            // CEmitter prints FP constants with std::to_string, i.e. "%f" (cemitter.cpp:104-105)
+            char buf[512];
+            snprintf(buf, sizeof buf, "%f", c.val);
+            k.is_float = true;
+            k.f = strtod(buf, nullptr);
+        } else if (c.type.is_unsigned()) {
+            k.i = (long long)(unsigned long long)c.val;
+        } else {
+            k.i = (long long)c.val;
+        }
+        // one slot per distinct (kind, value): equal constants read the same slot, so the
+        // compiler can share the comparisons that use them
+        int i = -1;
+        for (size_t j = 0; j < plan_.consts.size(); j++) {
+            auto& q = plan_.consts[j];
+            if (q.is_float == k.is_float && (k.is_float ? (memcmp(&q.f, &k.f, 8) == 0) : q.i == k.i)) i = (int)j;
+        }
+        if (i < 0) {
+            if (plan_.consts.size() >= (size_t)RF_MAX_CONSTS_) throw LowerError("too many constants");
+            i = (int)plan_.consts.size();
+            plan_.consts.push_back(k);
+        }
+        if (c.type.btype == FLOAT64) return "P.k[" + std::to_string(i) + "].f";
+        if (c.type.btype == FLOAT32) return "((float)P.k[" + std::to_string(i) + "].f)";
+        return "((" + ctype(c.type) + ")P.k[" + std::to_string(i) + "].i)";
+    }
+
+    void note_col(int input, size_t col)
+    {
+        auto& v = plan_.cols_read[input];
+        if (std::find(v.begin(), v.end(), (int)col) == v.end()) v.push_back((int)col);
+    }
+
+    // ---------------------------------------------------------------- expression emitter
+    struct Scope {
+        std::map<const ExprNode*, Val> bind;
+    };
+
+    struct Emitter {
+        Lowerer& L;
+        std::vector<Scope> scopes{1};
+        std::vector<std::string> decls;  // lazy symbol closures, in dependency order
+        std::map<std::pair<const ExprNode*, const ExprNode*>, std::string> vec_iter_idx;
+        std::map<std::string, std::string> locate_cache;
+        int counter = 0;
+        bool in_bounds_rows = true;
+
+        explicit Emitter(Lowerer& l) : L(l) {}
+
+        std::string fresh(const std::string& b) { return b + std::to_string(counter++); }
+        void bind(const Expr& s, Val v) { scopes.back().bind[s.get()] = std::move(v); }
+        const Val* lookup(const ExprNode* s) const
+        {
+            for (auto it = scopes.rbegin(); it != scopes.rend(); ++it) {
+                auto f = it->bind.find(s);
+                if (f != it->bind.end()) return &f->second;
+            }
+            return nullptr;
+        }
+
+        Val scalar(const std::string& c, const DataType& t)
+        {
+            Val v;
+            v.c = c;
+            v.type = t;
+            return v;
+        }
+
+        // a table symbol of primitive type becomes a lazily evaluated, cached closure, so
+        // short-circuit conditions keep skipping expensive probes and each value is computed once
+        Val lazy(const std::string& base, const Val& v, const DataType& t)
+        {
+            if (v.k != Val::SCALAR) return v;
+            std::string nm = fresh("lz_" + base + "_");
+            std::string ty = ctype(t);
+            decls.push_back(ty + " " + nm + "_v; bool " + nm + "_h = false; auto " + nm + " = [&]() -> " + ty +
+                            " { if (!" + nm + "_h) { " + nm + "_h = true; " + nm + "_v = (" + ty + ")(" + v.c +
+                            "); } return " + nm + "_v; };");
+            return scalar(nm + "()", t);
+        }
+
+        Val ev(const Expr& e)
+        {
+            switch (e->kind) {
+                case NodeKind::SYM: {
+                    if (auto b = lookup(e.get())) return *b;
+                    auto sym = std::static_pointer_cast<SymNode>(e);
+                    auto it = L.fn_->tbl.find(sym);
+                    if (it == L.fn_->tbl.end()) throw LowerError("unbound symbol " + sym->name, false);
+                    Val v = ev(it->second);
+                    if (v.k == Val::SCALAR) {
+                        std::string base;
+                        for (char ch : sym->name) base += isalnum((unsigned char)ch) ? ch : '_';
+                        v = lazy(base, v, sym->type);
+                    }
+                    scopes.front().bind[e.get()] = v;
+                    return v;
+                }
+                case NodeKind::CONST: return scalar(L.konst(*as<Const>(e)), e->type);
+                case NodeKind::NARY: return nary(*as<NaryExpr>(e));
+                case NodeKind::SELECT: {
+                    auto s = as<Select>(e);
+                    Val c = ev(s->cond);
+                    return sel(c.c, ev(s->true_body), ev(s->false_body));
+                }
+                case NodeKind::CAST: {
+                    auto c = as<Cast>(e);
+                    return scalar("((" + ctype(c->type) + ")(" + ev(c->arg).c + "))", c->type);
+                }
+                case NodeKind::GET: {
+                    auto g = as<Get>(e);
+                    Val v = ev(g->val);
+                    if (v.k == Val::STRUCT) return v.f.at(g->col);
+                    return v;
+                }
+                case NodeKind::NEW: {
+                    Val v;
+                    v.k = Val::STRUCT;
+                    v.type = e->type;
+                    for (auto& x : as<New>(e)->vals) v.f.push_back(ev(x));
+                    return v;
+                }
+                case NodeKind::ELEMENT: return element(*as<Element>(e));
+                case NodeKind::SUBVECTOR: {
+                    auto s = as<SubVector>(e);
+                    Val v = ev(s->vec);
+                    if (v.k != Val::VEC) throw LowerError("subvector of a non-input vector");
+                    Val r;
+                    r.k = Val::SUBVEC;
+                    r.slot = v.slot;
+                    r.input = v.input;
+                    r.vnode = v.vnode;
+                    r.type = e->type;
+                    r.s = ev(s->start).c;
+                    r.e = ev(s->end).c;
+                    return r;
+                }
+                case NodeKind::LENGTH: {
+                    auto l = as<Length>(e);
+                    Val v = ev(l->vec);
+                    if (v.k != Val::VEC) throw LowerError("length of a non-input vector");
+                    return scalar("P.t[" + std::to_string(v.slot) + "].col[" + std::to_string(l->col) + "].len", e->type);
+                }
+                case NodeKind::LOCATE: {
+                    auto l = as<Locate>(e);
+                    Val v = ev(l->vec);
+                    if (v.k != Val::VEC) throw LowerError("locate in a non-input vector");
+                    return scalar(locate(v, ev(l->iter).c), e->type);
+                }
+                case NodeKind::READDATA: {
+                    auto r = as<ReadData>(e);
+                    Val v = ev(r->vec);
+                    if (v.k != Val::VEC) throw LowerError("readdata of a non-input vector");
+                    L.note_col(v.input, r->col);
+                    return scalar("rf_rd<" + ctype(r->type) + ">(P.t[" + std::to_string(v.slot) + "].col[" +
+                                      std::to_string(r->col) + "], (long long)(" + ev(r->idx).c + "))",
+                                  r->type);
+                }
+                case NodeKind::IN: throw LowerError("In outside an Op predicate");
+                case NodeKind::OP: throw LowerError("a nested Op inside an expression is not lowered");
+                case NodeKind::REDUCE: throw LowerError("a Reduce nested inside this expression is not lowered");
+            }
+            throw LowerError("unknown node");
+        }
+
+        std::string locate(const Val& vec, const std::string& key)
+        {
+            L.plan_.needs_index[vec.input] = 1;
+            L.note_col(vec.input, 0);
+            std::string call = "rf_locate(P.t[" + std::to_string(vec.slot) + "].ix, (long long)(" + key + "))";
+            auto it = locate_cache.find(call);
+            if (it != locate_cache.end()) return it->second;
+            Val v = lazy("loc", scalar(call, types::IDX_T), types::IDX_T);
+            locate_cache[call] = v.c;
+            return v.c;
+        }
+
+        Val sel(const std::string& c, const Val& a, const Val& b)
+        {
+            if (a.k == Val::STRUCT) {
+                Val v;
+                v.k = Val::STRUCT;
+                v.type = a.type;
+                for (size_t i = 0; i < a.f.size(); i++) v.f.push_back(sel(c, a.f[i], b.f[i]));
+                return v;
+            }
+            return scalar("(" + c + " ? " + a.c + " : " + b.c + ")", a.type);
+        }
+
+        Val element(const Element& el)
+        {
+            Val vec = ev(el.vec);
+            if (vec.k != Val::VEC) throw LowerError("element of a non-input vector");
+            std::string idx;
+            bool inb = false;
+            auto key = std::make_pair(el.vec.get(), el.iter.get());
+            auto f = vec_iter_idx.find(key);
+            if (f != vec_iter_idx.end()) {
+                idx = f->second;
+                inb = in_bounds_rows;
+            } else {
+                idx = locate(vec, ev(el.iter).c);
+            }
+            const DataType& vt = vec.type;
+            if (vt.dim == 1) {
+                Val v;
+                v.k = Val::STRUCT;
+                v.type = el.type;
+                for (size_t c = vt.dim; c < vt.dtypes.size(); c++) {
+                    L.note_col(vec.input, c);
+                    std::string col = "P.t[" + std::to_string(vec.slot) + "].col[" + std::to_string(c) + "]";
+                    if (inb)
+                        v.f.push_back(scalar("rf_ld<" + ctype(vt.dtypes[c]) + ">(" + col + ".data, " + idx + ")", vt.dtypes[c]));
+                    else
+                        v.f.push_back(scalar("rf_rd<" + ctype(vt.dtypes[c]) + ">(" + col + ", " + idx + ")", vt.dtypes[c]));
+                }
+                return v;
+            }
+            if (vt.dim == 2) {
+                if (vt.encodings[0] != RUNEND) throw LowerError("a 2-d element needs a run-end encoded column 0");
+                Val r;
+                r.k = Val::SUBVEC;
+                r.slot = vec.slot;
+                r.input = vec.input;
+                r.vnode = vec.vnode;
+                r.type = el.type;
+                std::string c0 = "P.t[" + std::to_string(vec.slot) + "].col[0]";
+                r.s = "rf_runend(" + c0 + ", (" + idx + ") - 1)";
+                r.e = "rf_runend(" + c0 + ", " + idx + ")";
+                return r;
+            }
+            throw LowerError("Only support 1d and 2d vectors");
+        }
+
+        Val nary(const NaryExpr& n)
+        {
+            auto a = [&](size_t i) { return ev(n.args[i]).c; };
+            const std::string T = n.type.is_primitive() ? ctype(n.type) : "";
+            switch (n.op) {
+                case MathOp::ADD: return scalar("(" + a(0) + " + " + a(1) + ")", n.type);
+                case MathOp::SUB: return scalar("(" + a(0) + " - " + a(1) + ")", n.type);
+                case MathOp::MUL: return scalar("(" + a(0) + " * " + a(1) + ")", n.type);
+                case MathOp::DIV: return scalar("(" + a(0) + " / " + a(1) + ")", n.type);
+                case MathOp::MOD: return scalar("(" + a(0) + " % " + a(1) + ")", n.type);
+                case MathOp::MAX: return scalar("rf_max<" + T + ">(" + a(0) + ", " + a(1) + ")", n.type);
+                case MathOp::MIN: return scalar("rf_min<" + T + ">(" + a(0) + ", " + a(1) + ")", n.type);
+                case MathOp::LT: return scalar("(" + a(0) + " < " + a(1) + ")", n.type);
+                case MathOp::LTE: return scalar("(" + a(0) + " <= " + a(1) + ")", n.type);
+                case MathOp::GT: return scalar("(" + a(0) + " > " + a(1) + ")", n.type);
+                case MathOp::GTE: return scalar("(" + a(0) + " >= " + a(1) + ")", n.type);
+                case MathOp::EQ: return scalar("(" + a(0) + " == " + a(1) + ")", n.type);
+                case MathOp::NOT: return scalar("(!" + a(0) + ")", n.type);
+                case MathOp::AND: return scalar("(" + a(0) + " && " + a(1) + ")", n.type);
+                case MathOp::OR: return scalar("(" + a(0) + " || " + a(1) + ")", n.type);
+                case MathOp::NEG: return scalar("(-" + a(0) + ")", n.type);
+                case MathOp::SQRT: return scalar("sqrt(" + a(0) + ")", n.type);
+                case MathOp::CEIL: return scalar("ceil(" + a(0) + ")", n.type);
+                case MathOp::FLOOR: return scalar("floor(" + a(0) + ")", n.type);
+                case MathOp::POW: return scalar("pow(" + a(0) + ", " + a(1) + ")", n.type);
+                case MathOp::ABS:
+                    if (n.type.is_float()) return scalar("fabs(" + a(0) + ")", n.type);
+                    return scalar("((" + T + ")llabs((long long)(" + a(0) + ")))", n.type);
+                default: throw LowerError(std::string("operator not lowered: ") + mathop_name(n.op));
+            }
+        }
+    };
+
+    Val input_val(int i)
+    {
+        auto& s = fn_->inputs[i];
+        Val v;
+        v.type = s->type;
+        if (s->type.is_vector()) {
+            v.k = Val::VEC;
+            v.slot = plan_.table_slot[i];
+            v.input = i;
+            v.vnode = s.get();
+        } else {
+            int j = plan_.scalar_slot[i];
+            if (s->type.is_float())
+                v.c = "((" + ctype(s->type) + ")__longlong_as_double(P.s[" + std::to_string(j) + "]))";
+            else
+                v.c = "((" + ctype(s->type) + ")P.s[" + std::to_string(j) + "])";
+        }
+        return v;
+    }
+
+    void bind_inputs(Emitter& E)
+    {
+        for (size_t i = 0; i < fn_->inputs.size(); i++) E.bind(fn_->inputs[i], input_val((int)i));
+    }
+
+    // host-evaluable expression (loop bounds)
+    HostExpr host_expr(const Expr& e0)
+    {
+        Expr e = resolve(e0);
+        HostExpr h;
+        switch (e->kind) {
+            case NodeKind::CONST:
+                h.kind = HostExpr::CONST;
+                h.value = (long long)as<Const>(e)->val;
+                return h;
+            case NodeKind::LENGTH: {
+                auto l = as<Length>(e);
+                auto it = input_index_.find(resolve(l->vec).get());
+                if (it == input_index_.end()) throw LowerError("loop bound: length of a non-input vector");
+                h.kind = HostExpr::LEN;
+                h.input = it->second;
+                h.col = (int)l->col;
+                return h;
+            }
+            case NodeKind::SYM: {
+                auto it = input_index_.find(e.get());
+                if (it == input_index_.end() || !e->type.is_primitive()) throw LowerError("loop bound: unknown symbol");
+                h.kind = HostExpr::SCALAR;
+                h.input = it->second;
+                return h;
+            }
+            case NodeKind::CAST: return host_expr(as<Cast>(e)->arg);
+            case NodeKind::NARY: {
+                auto n = as<NaryExpr>(e);
+                switch (n->op) {
+                    case MathOp::ADD: h.kind = HostExpr::ADD; break;
+                    case MathOp::SUB: h.kind = HostExpr::SUB; break;
+                    case MathOp::MUL: h.kind = HostExpr::MUL; break;
+                    case MathOp::MAX: h.kind = HostExpr::MAX; break;
+                    case MathOp::MIN: h.kind = HostExpr::MIN; break;
+                    default: throw LowerError("loop bound: operator not evaluable on the host");
+                }
+                for (auto& a : n->args) h.args.push_back(host_expr(a));
+                return h;
+            }
+            default: throw LowerError("loop bound not evaluable on the host");
+        }
+    }
+
+    // ---------------------------------------------------------------- iteration space
+    bool affine(const Expr& e, const std::set<const ExprNode*>& vars)
+    {
+        switch (e->kind) {
+            case NodeKind::CONST: return true;
+            case NodeKind::SYM: return vars.count(e.get()) > 0;
+            case NodeKind::NARY: {
+                auto n = as<NaryExpr>(e);
+                if (n->op == MathOp::ADD || n->op == MathOp::SUB) return affine(n->args[0], vars) && affine(n->args[1], vars);
+                if (n->op == MathOp::NEG) return affine(n->args[0], vars);
+                if (n->op == MathOp::MUL)
+                    return (is_kind(n->args[0], NodeKind::CONST) && affine(n->args[1], vars)) ||
+                           (is_kind(n->args[1], NodeKind::CONST) && affine(n->args[0], vars));
+                return false;
+            }
+            default: return false;
+        }
+    }
+
+    // Reffine::visit + Reffine::extract_bound restated for `iter <op> affine(vars)`
+    void space_of(const Expr& pred, const Expr& iter, const std::set<const ExprNode*>& vars, Space& sp)
+    {
+        if (is_nary(pred, MathOp::AND)) {
+            space_of(as<NaryExpr>(pred)->args[0], iter, vars, sp);
+            space_of(as<NaryExpr>(pred)->args[1], iter, vars, sp);
+            return;
+        }
+        if (pred->kind == NodeKind::NARY) {
+            auto n = as<NaryExpr>(pred);
+            if (n->op == MathOp::OR) throw LowerError("union iteration spaces are not lowered");
+            if (n->op == MathOp::LT || n->op == MathOp::LTE || n->op == MathOp::GT || n->op == MathOp::GTE) {
+                Expr a = n->args[0], b = n->args[1];
+                MathOp op = n->op;
+                Expr rhs;
+                if (a.get() == iter.get() && !mentions(b, iter.get(), fn_->tbl)) {
+                    rhs = b;
+                } else if (b.get() == iter.get() && !mentions(a, iter.get(), fn_->tbl)) {
+                    rhs = a;
+                    op = op == MathOp::LT ? MathOp::GT : op == MathOp::LTE ? MathOp::GTE : op == MathOp::GT ? MathOp::LT : MathOp::LTE;
+                } else if (!mentions(pred, iter.get(), fn_->tbl)) {
+                    return;  // no bound solves the forall query: universal space, predicate dropped
+                } else {
+                    throw LowerError("iterator bound form not lowered");
+                }
+                if (!affine(rhs, vars) || !(iter->type.is_int() || iter->type.is_idx())) return;  // universal
+                auto one = std::make_shared<Const>(iter->type, 1.0);
+                if (op == MathOp::GTE) sp.lbs.push_back(rhs);
+                else if (op == MathOp::GT) sp.lbs.push_back(reffiner::_add(rhs, one));
+                else if (op == MathOp::LTE) sp.ubs.push_back(rhs);
+                else sp.ubs.push_back(reffiner::_sub(rhs, one));
+                return;
+            }
+            throw LowerError(std::string("Operator not supported by Reffine: ") + mathop_name(n->op));
+        }
+        if (pred->kind == NodeKind::SYM) {
+            if (pred.get() == iter.get()) return;
+            auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(pred));
+            if (it == fn_->tbl.end()) throw LowerError("Unable to reffine symbol");
+            if (pred->type == types::BOOL_T) {
+                sp.filters.push_back(pred);
+                return;
+            }
+            space_of(it->second, iter, vars, sp);
+            return;
+        }
+        if (pred->kind == NodeKind::IN) {
+            auto in = as<In>(pred);
+            if (in->iter.get() != iter.get()) throw LowerError("In over another iterator");
+            Expr vec = resolve(in->vec);
+            auto f = input_index_.find(vec.get());
+            if (f == input_index_.end()) throw LowerError("iteration over a non-input vector");
+            sp.n_vecs++;
+            sp.has_vec = true;
+            sp.vec_input = f->second;
+            sp.vec_node = in->vec;
+            return;
+        }
+        throw LowerError("predicate node not lowered");
+    }
+
+    Space op_space(const Op& op)
+    {
+        if (op.iters.size() != 1) throw LowerError("multi-iterator Op");
+        Space sp;
+        sp.iter = op.iters[0];
+        std::set<const ExprNode*> vars;
+        for (auto& s : fn_->inputs)
+            if (s->type.is_val()) vars.insert(s.get());
+        space_of(op.pred, sp.iter, vars, sp);
+        if (sp.n_vecs > 1) throw LowerError("merge co-iteration is lowered by the join template");
+        if (!sp.has_vec && sp.lbs.empty()) throw LowerError("unbounded iteration space (no lower bound)");
+        if (!sp.has_vec && sp.ubs.empty()) throw LowerError("unbounded iteration space (no upper bound)");
+        return sp;
+    }
+
+    // combine bounds as the LBound/UBound chain does: L = max(lbs..., base lb), U = min(ubs..., base ub)
+    std::string bound_expr(Emitter& E, const std::vector<Expr>& bs, const std::string& base, bool is_max,
+                           const DataType& t)
+    {
+        std::string r = base;
+        for (auto& b : bs) {
+            std::string c = "((" + ctype(t) + ")(" + E.ev(b).c + "))";
+            r = r.empty() ? c : (std::string(is_max ? "rf_max<" : "rf_min<") + ctype(t) + ">(" + c + ", " + r + ")");
+        }
+        return r;
+    }
+
+    // ---------------------------------------------------------------- Reduce analysis
+    std::map<std::vector<size_t>, Expr> leaf_syms_;
+    std::map<const ExprNode*, std::vector<size_t>> leaf_path_;
+
+    Expr leaf_sym(const std::vector<size_t>& path, const DataType& t)
+    {
+        auto it = leaf_syms_.find(path);
+        if (it != leaf_syms_.end()) return it->second;
+        std::string nm = "$state";
+        for (auto p : path) nm += "." + std::to_string(p);
+        auto s = std::make_shared<SymNode>(nm, t);
+        leaf_syms_[path] = s;
+        leaf_path_[s.get()] = path;
+        return s;
+    }
+
+    // Get(...(state)...) chains become leaf symbols; Get(New)/Get(Select) are simplified
+    Expr simplify(const Expr& e, const Reduce& red)
+    {
+        if (e.get() == red.state.get()) {
+            if (red.state->type.is_struct()) return e;
+            return leaf_sym({}, red.state->type);
+        }
+        switch (e->kind) {
+            case NodeKind::GET: {
+                auto g = as<Get>(e);
+                Expr v = simplify(g->val, red);
+                if (v.get() == red.state.get()) return leaf_sym({g->col}, e->type);
+                auto lp = leaf_path_.find(v.get());
+                if (lp != leaf_path_.end() && v->type.is_struct()) {
+                    auto p = lp->second;
+                    p.push_back(g->col);
+                    return leaf_sym(p, e->type);
+                }
+                if (v->kind == NodeKind::NEW) return simplify(as<New>(v)->vals.at(g->col), red);
+                if (v->kind == NodeKind::SELECT) {
+                    auto s = as<Select>(v);
+                    return std::make_shared<Select>(s->cond, simplify(std::make_shared<Get>(s->true_body, g->col), red),
+                                                    simplify(std::make_shared<Get>(s->false_body, g->col), red));
+                }
+                if (v->kind == NodeKind::SYM && v->type.is_struct()) {
+                    auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(v));
+                    if (it != fn_->tbl.end() && mentions(it->second, red.state.get(), fn_->tbl))
+                        return simplify(std::make_shared<Get>(it->second, g->col), red);
+                }
+                if (v.get() == g->val.get()) return e;
+                return std::make_shared<Get>(v, g->col);
+            }
+            case NodeKind::SELECT: {
+                auto s = as<Select>(e);
+                if (!mentions(e, red.state.get(), fn_->tbl)) return e;
+                return std::make_shared<Select>(simplify(s->cond, red), simplify(s->true_body, red),
+                                                simplify(s->false_body, red));
+            }
+            case NodeKind::NARY: {
+                auto n = as<NaryExpr>(e);
+                if (!mentions(e, red.state.get(), fn_->tbl)) return e;
+                std::vector<Expr> args;
+                for (auto& a : n->args) args.push_back(simplify(a, red));
+                return std::make_shared<NaryExpr>(n->type, n->op, args);
+            }
+            case NodeKind::NEW: {
+                if (!mentions(e, red.state.get(), fn_->tbl)) return e;
+                std::vector<Expr> v;
+                for (auto& x : as<New>(e)->vals) v.push_back(simplify(x, red));
+                return std::make_shared<New>(v);
+            }
+            case NodeKind::CAST: {
+                if (!mentions(e, red.state.get(), fn_->tbl)) return e;
+                return std::make_shared<Cast>(e->type, simplify(as<Cast>(e)->arg, red));
+            }
+            case NodeKind::SYM: {
+                if (e->type.is_struct() || !mentions(e, red.state.get(), fn_->tbl)) return e;
+                auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(e));
+                if (it != fn_->tbl.end()) return simplify(it->second, red);
+                return e;
+            }
+            default: return e;
+        }
+    }
+
+    Expr field(const Expr& e, const std::vector<size_t>& path, const Reduce& red)
+    {
+        Expr x = e;
+        for (auto p : path) x = simplify(std::make_shared<Get>(x, p), red);
+        return simplify(x, red);
+    }
+
+    bool mentions_state(const Expr& e)
+    {
+        std::set<const ExprNode*> t, seen;
+        for (auto& kv : leaf_syms_) t.insert(kv.second.get());
+        return mentions(e, t, fn_->tbl, seen);
+    }
+
+    void collect_leaves(const Reduce& red, const DataType& t, std::vector<size_t> path, std::vector<Leaf>& out)
+    {
+        if (t.is_struct()) {
+            for (size_t i = 0; i < t.dtypes.size(); i++) {
+                auto p = path;
+                p.push_back(i);
+                collect_leaves(red, t.dtypes[i], p, out);
+            }
+            return;
+        }
+        if (!t.is_primitive()) throw LowerError("reduce state must be primitives and structs");
+        Leaf lf;
+        lf.path = path;
+        lf.type = t;
+        Expr ls = leaf_sym(path, t);
+        Expr E = field(red.acc_expr, path, red);
+        lf.init = path.empty() ? red.init_expr : field(red.init_expr, path, red);
+        // peel conditional updates: sel(c, update, s) / sel(c, s, update)
+        Expr cond;
+        auto conj = [&](Expr c) { cond = cond ? Expr(reffiner::_and(cond, c)) : c; };
+        for (;;) {
+            if (E->kind != NodeKind::SELECT) break;
+            auto s = as<Select>(E);
+            if (s->false_body.get() == ls.get()) {
+                conj(s->cond);
+                E = s->true_body;
+            } else if (s->true_body.get() == ls.get()) {
+                conj(reffiner::_not(s->cond));
+                E = s->false_body;
+            } else {
+                throw LowerError("reduce accumulator field is not a conditional update of itself");
+            }
+        }
+        if (E.get() == ls.get()) {
+            lf.op = AggOp::NONE;
+        } else if (E->kind == NodeKind::NARY) {
+            auto n = as<NaryExpr>(E);
+            auto a0 = n->args[0];
+            auto a1 = n->args.size() > 1 ? n->args[1] : nullptr;
+            switch (n->op) {
+                case MathOp::ADD: {
+                    // s + e, e + s, or a left-leaning chain s + e1 + e2 ...
+                    std::vector<Expr> terms;
+                    std::function<void(const Expr&)> chain = [&](const Expr& x) {
+                        if (is_nary(x, MathOp::ADD)) {
+                            chain(as<NaryExpr>(x)->args[0]);
+                            terms.push_back(as<NaryExpr>(x)->args[1]);
+                        } else {
+                            terms.push_back(x);
+                        }
+                    };
+                    if (a1 && a1.get() == ls.get()) {
+                        lf.value = a0;
+                    } else {
+                        chain(E);
+                        if (terms.empty() || terms[0].get() != ls.get())
+                            throw LowerError("reduce sum is not of the form state + value");
+                        Expr v = terms[1];
+                        for (size_t i = 2; i < terms.size(); i++) v = reffiner::_add(v, terms[i]);
+                        lf.value = v;
+                    }
+                    lf.op = AggOp::SUM;
+                    break;
+                }
+                case MathOp::SUB:
+                    if (a0.get() != ls.get()) throw LowerError("reduce difference is not state - value");
+                    lf.value = reffiner::_neg(a1);
+                    lf.op = AggOp::SUM;
+                    break;
+                case MathOp::MAX: case MathOp::MIN: case MathOp::OR: case MathOp::AND:
+                    if (a0.get() == ls.get()) {
+                        lf.value = a1;
+                    } else if (a1.get() == ls.get()) {
+                        lf.value = a0;
+                        lf.state_first = false;
+                    } else {
+                        throw LowerError("reduce min/max/or/and does not take the state");
+                    }
+                    lf.op = n->op == MathOp::MAX ? AggOp::MAX : n->op == MathOp::MIN ? AggOp::MIN
+                            : n->op == MathOp::OR ? AggOp::OR : AggOp::AND;
+                    break;
+                default: throw LowerError(std::string("reduce update operator not associative: ") + mathop_name(n->op));
+            }
+        } else {
+            throw LowerError("reduce accumulator field is not an associative update");
+        }
+        lf.cond = cond;
+        if (lf.op != AggOp::NONE) {
+            if (mentions_state(lf.value) || (cond && mentions_state(cond)))
+                throw LowerError("reduce update reads another state field");
+            if (lf.op == AggOp::SUM && lf.value->kind == NodeKind::CONST && as<Const>(lf.value)->val == 1.0)
+                lf.count = true;
+            if (lf.op == AggOp::SUM && lf.type.btype == BOOL) throw LowerError("sum over bool");
+        }
+        if (mentions_state(lf.init)) throw LowerError("reduce init reads the state");
+        out.push_back(lf);
+    }
+
+    // ---------------------------------------------------------------- grouping
+    // Leaves whose conditions share the same filter conjuncts and differ only in
+    // `key == constant` conjuncts over the same key expressions form dense groups.
+    bool detect_groups(std::vector<Leaf>& leaves, std::vector<std::vector<int>>& groups,
+                       std::vector<Expr>& key_exprs, std::vector<Expr>& filters)
+    {
+        std::vector<int> act;
+        for (size_t i = 0; i < leaves.size(); i++)
+            if (leaves[i].op != AggOp::NONE) act.push_back((int)i);
+        if (act.size() < 2) return false;
+        for (int i : act) {
+            auto& lf = leaves[i];
+            std::vector<Expr> cj;
+            if (lf.cond) flatten_and(lf.cond, cj);
+            for (auto& c : cj) {
+                if (is_nary(c, MathOp::EQ)) {
+                    auto n = as<NaryExpr>(c);
+                    if (n->args[1]->kind == NodeKind::CONST && n->args[0]->kind != NodeKind::CONST) {
+                        lf.keys.push_back({n->args[0], n->args[1]});
+                        continue;
+                    }
+                    if (n->args[0]->kind == NodeKind::CONST && n->args[1]->kind != NodeKind::CONST) {
+                        lf.keys.push_back({n->args[1], n->args[0]});
+                        continue;
+                    }
+                }
+                lf.filters.push_back(c);
+            }
+        }
+        auto& l0 = leaves[act[0]];
+        if (l0.keys.empty()) return false;
+        // order keys by the first leaf's order; every leaf must have the same key expressions
+        for (auto& kv : l0.keys) key_exprs.push_back(kv.first);
+        for (int i : act) {
+            auto& lf = leaves[i];
+            if (lf.keys.size() != key_exprs.size() || lf.filters.size() != l0.filters.size()) return false;
+            std::vector<std::pair<Expr, Expr>> ordered;
+            for (auto& ke : key_exprs) {
+                bool found = false;
+                for (auto& kv : lf.keys)
+                    if (same(kv.first, ke)) {
+                        ordered.push_back(kv);
+                        found = true;
+                        break;
+                    }
+                if (!found) return false;
+            }
+            lf.keys = ordered;
+            for (auto& f : lf.filters) {
+                bool found = false;
+                for (auto& g : l0.filters)
+                    if (same(f, g)) found = true;
+                if (!found) return false;
+            }
+        }
+        filters = l0.filters;
+        // partition by constant tuple, in first-appearance order
+        std::vector<std::vector<double>> tuples;
+        for (int i : act) {
+            std::vector<double> t;
+            for (auto& kv : leaves[i].keys) t.push_back(as<Const>(kv.second)->val);
+            size_t g = 0;
+            for (; g < tuples.size(); g++)
+                if (tuples[g] == t) break;
+            if (g == tuples.size()) {
+                tuples.push_back(t);
+                groups.emplace_back();
+            }
+            groups[g].push_back(i);
+        }
+        if (groups.size() < 2 || groups.size() > (size_t)RF_MAX_GROUPS_) return false;
+        // every group must aggregate the same sequence of (op, type, value)
+        auto& g0 = groups[0];
+        for (auto& g : groups) {
+            if (g.size() != g0.size()) return false;
+            for (size_t m = 0; m < g.size(); m++) {
+                auto &a = leaves[g[m]], &b = leaves[g0[m]];
+                if (a.op != b.op || a.type != b.type || a.count != b.count || a.state_first != b.state_first ||
+                    !same(a.value, b.value))
+                    return false;
+            }
+        }
+        return true;
+    }
+    static constexpr int RF_MAX_GROUPS_ = 64;
+
+    // ---------------------------------------------------------------- code generation helpers
+    static std::string acc_ctype(const Leaf& lf)
+    {
+        if (lf.count) return "long long";
+        if (lf.type.btype == BOOL) return "long long";
+        if (lf.type.is_float()) return lf.type.btype == FLOAT32 ? "float" : "double";
+        if (lf.type.is_unsigned()) return "unsigned long long";
+        return "long long";
+    }
+
+    // identity for sums; for idempotent ops every partial starts at the init value
+    std::string acc_start(Emitter& E, const Leaf& lf)
+    {
+        if (lf.op == AggOp::SUM) return "0";
+        return "(" + acc_ctype(lf) + ")(" + E.ev(lf.init).c + ")";
+    }
+
+    static std::string combine_expr(const Leaf& lf, const std::string& a, const std::string& b)
+    {
+        switch (lf.op) {
+            case AggOp::SUM: return "(" + a + " + " + b + ")";
+            case AggOp::MAX: return lf.state_first ? "((" + a + " < " + b + ") ? " + b + " : " + a + ")"
+                                                   : "((" + b + " < " + a + ") ? " + a + " : " + b + ")";
+            case AggOp::MIN: return lf.state_first ? "((" + b + " < " + a + ") ? " + b + " : " + a + ")"
+                                                   : "((" + a + " < " + b + ") ? " + a + " : " + b + ")";
+            case AggOp::OR: return "(long long)((" + a + ") || (" + b + "))";
+            case AggOp::AND: return "(long long)((" + a + ") && (" + b + "))";
+            default: return a;
+        }
+    }
+
+    // final state value of a leaf from its folded accumulator `tot`
+    std::string final_leaf(Emitter& E, const Leaf& lf, const std::string& tot)
+    {
+        std::string T = ctype(lf.type);
+        if (lf.op == AggOp::NONE) return "((" + T + ")(" + E.ev(lf.init).c + "))";
+        if (lf.op == AggOp::SUM) return "((" + T + ")((" + E.ev(lf.init).c + ") + (" + T + ")(" + tot + ")))";
+        return "((" + T + ")(" + tot + "))";
+    }
+
+    // evaluates the Func output with the Reduce bound to its final state; stores in C layout
+    void emit_output_store(Emitter& E, std::ostringstream& o, const Reduce& red,
+                           const std::map<std::vector<size_t>, std::string>& finals)
+    {
+        std::function<Val(const DataType&, std::vector<size_t>)> mk = [&](const DataType& t, std::vector<size_t> p) {
+            if (t.is_struct()) {
+                Val v;
+                v.k = Val::STRUCT;
+                v.type = t;
+                for (size_t i = 0; i < t.dtypes.size(); i++) {
+                    auto q = p;
+                    q.push_back(i);
+                    v.f.push_back(mk(t.dtypes[i], q));
+                }
+                return v;
+            }
+            Val v;
+            v.c = finals.at(p);
+            v.type = t;
+            return v;
+        };
+        Val st = mk(red.type, {});
+        // bind every symbol whose table entry is this Reduce
+        for (auto& kv : fn_->tbl)
+            if (resolve(kv.first).get() == (const ExprNode*)&red) E.bind(kv.first, st);
+        Expr outx = fn_->output;
+        Val ov;
+        if ((const ExprNode*)resolve(outx).get() == (const ExprNode*)&red) ov = st;
+        else ov = E.ev(outx);
+        for (auto& d : E.decls) o << "    " << d << "\n";
+        E.decls.clear();
+        size_t off = 0;
+        store_c(o, ov, plan_.out_type, off, "out");
+        plan_.out_size = c_size(plan_.out_type);
+    }
+
+    void store_c(std::ostringstream& o, const Val& v, const DataType& t, size_t& off, const std::string& base)
+    {
+        if (t.is_struct()) {
+            size_t al = c_align(t);
+            off = (off + al - 1) / al * al;
+            size_t start = off;
+            for (size_t i = 0; i < t.dtypes.size(); i++) store_c(o, v.f.at(i), t.dtypes[i], off, base);
+            off = start + c_size(t);
+            return;
+        }
+        size_t al = c_align(t);
+        off = (off + al - 1) / al * al;
+        o << "    *(" << ctype(t) << "*)(" << base << " + " << off << ") = (" << ctype(t) << ")(" << v.c << ");\n";
+        off += c_size(t);
+    }
+
+    // ---------------------------------------------------------------- driving loop of a Reduce
+    struct Drive {
+        bool subvec = false;
+        Space sp;
+        int input = -1;
+        int slot = -1;
+    };
+
+    // binds the reduce value symbol and emits the row prologue (validity / iteration condition);
+    // returns the row-condition expression
+    std::string bind_row(Emitter& E, const Reduce& red, const Drive& d, std::ostringstream& body)
+    {
+        bind_inputs(E);
+        std::string sl = std::to_string(d.slot);
+        if (d.subvec) {
+            // LoopGen::visit(Reduce) over a SubVector: value = columns 1..n-1, condition = validity
+            // of column 1 (loopgen.cpp:221-242)
+            const DataType& vt = fn_->inputs[d.input]->type;
+            Val v;
+            v.k = Val::STRUCT;
+            v.type = red.val->type;
+            for (size_t c = 1; c < vt.dtypes.size(); c++) {
+                v.f.push_back(E.scalar("rf_ld<" + ctype(vt.dtypes[c]) + ">(P.t[" + sl + "].col[" + std::to_string(c) +
+                                           "].data, r)",
+                                       vt.dtypes[c]));
+            }
+            E.bind(red.val, v);
+            pending_cols_ = true;
+            return "rf_valid(P.t[" + sl + "].col[1].valid, r)";
+        }
+        // Op iteration space (single iterator)
+        const auto& op = *as<Op>(red.vec);
+        const Space& sp = d.sp;
+        std::string it_c, cond;
+        std::string T = ctype(sp.iter->type);
+        if (sp.has_vec) {
+            note_col(d.input, 0);
+            it_c = "rf_ld<" + T + ">(P.t[" + sl + "].col[0].data, r)";
+            cond = "rf_valid(P.t[" + sl + "].col[0].valid, r)";
+            E.vec_iter_idx[{sp.vec_node.get(), sp.iter.get()}] = "r";
+        } else {
+            it_c = "((" + T + ")r)";
+            cond = "true";
+        }
+        body << "    const " << T << " it = " << it_c << ";\n";
+        E.bind(op.iters[0], E.scalar("it", sp.iter->type));
+        if (!sp.lbs.empty()) cond += " && (it >= (" + T + ")P.range[2])";
+        if (!sp.ubs.empty()) cond += " && (it <= (" + T + ")P.range[3])";
+        for (auto& f : sp.filters) cond += " && (" + E.ev(f).c + ")";
+        // value = (iterators..., outputs...)  (loopgen.cpp:88-91)
+        Val v;
+        v.k = Val::STRUCT;
+        v.type = red.val->type;
+        v.f.push_back(E.scalar("it", sp.iter->type));
+        for (auto& o : op.outputs) v.f.push_back(E.ev(o));
+        E.bind(red.val, v);
+        return cond;
+    }
+    bool pending_cols_ = false;
+
+    // range kernels of an Op iteration space: start = Locate(max(lbs, col0[0])) for a vector,
+    // end = first row past the upper bound (UBoundSpace::_is_alive stops the loop there)
+    void emit_range_kernels(std::ostringstream& o, const Drive& d)
+    {
+        const Space& sp = d.sp;
+        Emitter E(*this);
+        bind_inputs(E);
+        std::string T = ctype(sp.iter->type);
+        std::string sl = std::to_string(d.slot);
+        std::ostringstream b;
+        if (sp.has_vec) {
+            std::string first = "rf_rd<" + T + ">(P.t[" + sl + "].col[0], 0)";
+            std::string last = "rf_rd<" + T + ">(P.t[" + sl + "].col[0], P.t[" + sl + "].col[0].len - 1)";
+            std::string L = bound_expr(E, sp.lbs, first, true, sp.iter->type);
+            std::string U = sp.ubs.empty() ? "0" : bound_expr(E, sp.ubs, last, false, sp.iter->type);
+            plan_.needs_index[d.input] = 1;
+            b << "    const " << T << " L = " << L << ";\n";
+            b << "    const " << T << " U = " << U << ";\n";
+            b << "    long long start = P.t[" << sl << "].col[0].len > 0 ? rf_locate(P.t[" << sl << "].ix, (long long)L) : 0;\n";
+            b << "    long long end = P.t[" << sl << "].col[0].len;\n";
+            b << "    if (start < 0) { rf_set_err(P, RF_DEVERR_RANGE); start = end; }\n";
+        } else {
+            std::string L = bound_expr(E, sp.lbs, "", true, sp.iter->type);
+            std::string U = bound_expr(E, sp.ubs, "", false, sp.iter->type);
+            b << "    const " << T << " L = " << L << ";\n";
+            b << "    const " << T << " U = " << U << ";\n";
+            b << "    long long start = (long long)L;\n";
+            b << "    long long end = (long long)U + 1;\n";
+            b << "    if (end < start) end = start;\n";
+        }
+        o << "extern \"C\" __global__ void rf_range(const __grid_constant__ RfParams P)\n{\n";
+        o << "    if (threadIdx.x != 0 || blockIdx.x != 0) return;\n";
+        for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+        o << b.str();
+        o << "    P.range[0] = start;\n    P.range[1] = end;\n    P.range[2] = (long long)L;\n    P.range[3] = (long long)U;\n}\n\n";
+        plan_.kernels.push_back({"rf_range", 32, 0, KernelSpec::RANGE});
+        if (sp.has_vec && !sp.ubs.empty()) {
+            o << "extern \"C\" __global__ void __launch_bounds__(256) rf_stop(const __grid_constant__ RfParams P)\n{\n";
+            o << "    const long long start = P.range[0], n = P.t[" << sl << "].col[0].len;\n";
+            o << "    const " << T << " U = (" << T << ")P.range[3];\n";
+            o << "    for (long long r = start + blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;\n"
+              << "         r += (long long)gridDim.x * blockDim.x) {\n";
+            o << "        if (!(rf_ld<" << T << ">(P.t[" << sl << "].col[0].data, r) <= U)) { atomicMin(P.range + 1, r); break; }\n";
+            o << "    }\n}\n\n";
+            plan_.kernels.push_back({"rf_stop", 256, 0, KernelSpec::STOP});
+        }
+        plan_.device_range = true;
+    }
+
+    // ---------------------------------------------------------------- Reduce lowering
+    void lower_reduce(const Reduce& red)
+    {
+        Drive d;
+        if (red.vec->kind == NodeKind::OP) {
+            d.sp = op_space(*as<Op>(red.vec));
+            if (d.sp.has_vec) {
+                d.input = d.sp.vec_input;
+                d.slot = plan_.table_slot[d.input];
+                plan_.drive_input = d.input;
+                HostExpr lo;
+                lo.kind = HostExpr::CONST;
+                lo.value = 0;
+                HostExpr hi;
+                hi.kind = HostExpr::LEN;
+                hi.input = d.input;
+                hi.col = 0;
+                plan_.row_lo = lo;
+                plan_.row_hi = hi;
+            } else {
+                // range space: bounds are host-evaluable; the device range kernel still computes
+                // them (exactly as the loop would) and the host passes a safe tiling range
+                plan_.row_lo = minmax_host(d.sp.lbs, true);
+                HostExpr hi = minmax_host(d.sp.ubs, false);
+                HostExpr one;
+                one.kind = HostExpr::CONST;
+                one.value = 1;
+                HostExpr h2;
+                h2.kind = HostExpr::ADD;
+                h2.args = {hi, one};
+                plan_.row_hi = h2;
+            }
+        } else if (red.vec->kind == NodeKind::SUBVECTOR) {
+            auto sv = as<SubVector>(red.vec);
+            auto f = input_index_.find(resolve(sv->vec).get());
+            if (f == input_index_.end()) throw LowerError("reduce over a subvector of a non-input vector");
+            d.subvec = true;
+            d.input = f->second;
+            d.slot = plan_.table_slot[d.input];
+            plan_.drive_input = d.input;
+            plan_.row_lo = host_expr(sv->start);
+            plan_.row_hi = host_expr(sv->end);
+            note_col(d.input, 1);
+        } else {
+            throw LowerError("Unsupported reduction vector");  // loopgen.cpp:243-245
+        }
+
+        std::vector<Leaf> leaves;
+        collect_leaves(red, red.type, {}, leaves);
+        std::vector<std::vector<int>> groups;
+        std::vector<Expr> key_exprs, filters;
+        bool grouped = detect_groups(leaves, groups, key_exprs, filters);
+
+        std::ostringstream src;
+        src << "// generated by the reffine_gb300 lowering pass: " << fn_->name << "\n";
+        src << "#include \"rf_device.cuh\"\n\n";
+        if (!d.subvec) emit_range_kernels(src, d);
+
+        if (!grouped) gen_scan_reduce(src, red, d, leaves);
+        else gen_group_reduce(src, red, d, leaves, groups, key_exprs, filters);
+        plan_.source = src.str();
+    }
+
+    HostExpr minmax_host(const std::vector<Expr>& bs, bool is_max)
+    {
+        HostExpr r = host_expr(bs[0]);
+        for (size_t i = 1; i < bs.size(); i++) {
+            HostExpr h;
+            h.kind = is_max ? HostExpr::MAX : HostExpr::MIN;
+            h.args = {host_expr(bs[i]), r};
+            r = h;
+        }
+        return r;
+    }
+
+    // cost-ordered conjunction: cheap column predicates first, hash probes last
+    Expr order_conjuncts(const Expr& c)
+    {
+        std::vector<Expr> cj;
+        flatten_and(c, cj);
+        if (cj.size() < 2) return c;
+        std::function<int(const Expr&, std::set<const ExprNode*>&)> cost = [&](const Expr& e, std::set<const ExprNode*>& seen) -> int {
+            if (!e || seen.count(e.get())) return 0;
+            seen.insert(e.get());
+            int k = e->kind == NodeKind::LOCATE ? 100 : e->kind == NodeKind::READDATA ? 20 : 1;
+            if (e->kind == NodeKind::SYM) {
+                auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(e));
+                if (it != fn_->tbl.end()) return cost(it->second, seen);
+                return 0;
+            }
+            if (e->kind == NodeKind::ELEMENT) k = 20;
+            std::vector<Expr> ch;
+            children(e, ch);
+            for (auto& x : ch) k += cost(x, seen);
+            return k;
+        };
+        std::vector<std::pair<int, Expr>> v;
+        for (auto& x : cj) {
+            std::set<const ExprNode*> seen;
+            v.push_back({cost(x, seen), x});
+        }
+        std::stable_sort(v.begin(), v.end(), [](auto& a, auto& b) { return a.first < b.first; });
+        Expr r = v[0].second;
+        for (size_t i = 1; i < v.size(); i++) r = reffiner::_and(r, v[i].second);
+        return r;
+    }
+
+    void gen_scan_reduce(std::ostringstream& src, const Reduce& red, const Drive& d, std::vector<Leaf>& leaves)
+    {
+        plan_.kind = PlanKind::SCAN_REDUCE;
+        const int T = plan_.threads;
+        // accumulator struct: one 8-byte slot per active leaf
+        std::ostringstream acc, init, comb, shfl, row, fin;
+        std::vector<int> act;
+        for (size_t i = 0; i < leaves.size(); i++)
+            if (leaves[i].op != AggOp::NONE) act.push_back((int)i);
+        Emitter Ei(*this);
+        bind_inputs(Ei);
+        acc << "struct RfAcc {\n";
+        if (act.empty()) acc << "    long long unused;\n";
+        for (size_t k = 0; k < act.size(); k++) {
+            auto& lf = leaves[act[k]];
+            std::string ct = acc_ctype(lf);
+            if (ct == "float") ct = "double";  // keep 8-byte slots; f32 sums are rounded per update below
+            acc << "    " << ct << " a" << k << ";\n";
+        }
+        acc << "};\n\n";
+        init << "RF_DEV void rf_acc_init(const RfParams& P, RfAcc& A)\n{\n";
+        std::ostringstream initb;
+        for (size_t k = 0; k < act.size(); k++) initb << "    A.a" << k << " = " << acc_start(Ei, leaves[act[k]]) << ";\n";
+        for (auto& dcl : Ei.decls) init << "    " << dcl << "\n";
+        init << initb.str() << "}\n\n";
+        comb << "RF_DEV void rf_acc_combine(RfAcc& A, const RfAcc& B)\n{\n";
+        for (size_t k = 0; k < act.size(); k++) {
+            auto& lf = leaves[act[k]];
+            std::string a = "A.a" + std::to_string(k), b = "B.a" + std::to_string(k);
+            std::string e = combine_expr(lf, a, b);
+            if (lf.type.btype == FLOAT32 && lf.op == AggOp::SUM) e = "(double)((float)" + a + " + (float)" + b + ")";
+            comb << "    " << a << " = " << e << ";\n";
+        }
+        if (act.empty()) comb << "    (void)A; (void)B;\n";
+        comb << "}\n\n";
+        shfl << "RF_DEV RfAcc rf_acc_shfl(const RfAcc& A, int off)\n{\n    RfAcc R;\n";
+        for (size_t k = 0; k < act.size(); k++) shfl << "    R.a" << k << " = __shfl_down_sync(0xffffffffu, A.a" << k << ", off);\n";
+        if (act.empty()) shfl << "    R.unused = A.unused; (void)off;\n";
+        shfl << "    return R;\n}\n\n";
+
+        // row function
+        Emitter E(*this);
+        std::ostringstream body;
+        std::string rowcond = bind_row(E, red, d, body);
+        // leaves sharing a condition (structurally) are updated under one test of it
+        std::ostringstream upd;
+        std::vector<char> done(act.size(), 0);
+        for (size_t k = 0; k < act.size(); k++) {
+            if (done[k]) continue;
+            auto& lf = leaves[act[k]];
+            std::string cond = lf.cond ? E.ev(order_conjuncts(lf.cond)).c : "";
+            std::string ind = cond.empty() ? "    " : "        ";
+            if (!cond.empty()) upd << "    if (" << cond << ") {\n";
+            for (size_t j = k; j < act.size(); j++) {
+                auto& lj = leaves[act[j]];
+                if (done[j]) continue;
+                bool samec = (!lf.cond && !lj.cond) || (lf.cond && lj.cond && same(lf.cond, lj.cond));
+                if (!samec) continue;
+                done[j] = 1;
+                std::string a = "A.a" + std::to_string(j);
+                std::string val;
+                if (lj.count) val = "1";
+                else if (lj.op == AggOp::OR || lj.op == AggOp::AND) val = "(long long)(" + E.ev(lj.value).c + ")";
+                else val = "(" + ctype(lj.type) + ")(" + E.ev(lj.value).c + ")";
+                std::string e = combine_expr(lj, a, val);
+                if (lj.type.btype == FLOAT32 && lj.op == AggOp::SUM) e = "(double)((float)" + a + " + " + val + ")";
+                upd << ind << a << " = " << e << ";\n";
+            }
+            if (!cond.empty()) upd << "    }\n";
+        }
+        row << "RF_DEV void rf_row(const RfParams& P, long long r, RfAcc& A)\n{\n";
+        row << body.str();
+        for (auto& dcl : E.decls) row << "    " << dcl << "\n";
+        row << "    if (!(" << rowcond << ")) return;\n";
+        row << upd.str();
+        if (act.empty()) row << "    (void)A;\n";
+        row << "}\n\n";
+
+        // epilogue
+        Emitter Ef(*this);
+        bind_inputs(Ef);
+        std::map<std::vector<size_t>, std::string> finals;
+        std::ostringstream fb;
+        for (size_t i = 0, k = 0; i < leaves.size(); i++) {
+            auto& lf = leaves[i];
+            std::string tot = lf.op == AggOp::NONE ? "0" : "A.a" + std::to_string(k++);
+            std::string nm = "st" + std::to_string(i);
+            fb << "    const " << ctype(lf.type) << " " << nm << " = " << final_leaf(Ef, lf, tot) << ";\n";
+            finals[lf.path] = nm;
+        }
+        fin << "RF_DEV void rf_finish(const RfParams& P, const RfAcc& A, unsigned char* out)\n{\n";
+        std::ostringstream stores;
+        emit_output_store(Ef, stores, red, finals);
+        for (auto& dcl : Ef.decls) fin << "    " << dcl << "\n";
+        fin << fb.str() << stores.str() << "}\n\n";
+
+        src << acc.str() << init.str() << comb.str() << shfl.str() << row.str() << fin.str();
+        src << "#define RF_SCAN_REDUCE 1\n#include \"rf_templates.cuh\"\n";
+        src << "RF_SCAN_REDUCE_KERNEL(rf_main, " << T << ")\n";
+        plan_.kernels.push_back({"rf_main", T, 0, KernelSpec::MAIN});
+        plan_.acc_bytes = std::max<size_t>(8, act.size() * 8);
+    }
+
+    void gen_group_reduce(std::ostringstream& src, const Reduce& red, const Drive& d, std::vector<Leaf>& leaves,
+                          const std::vector<std::vector<int>>& groups, const std::vector<Expr>& key_exprs,
+                          const std::vector<Expr>& filters)
+    {
+        plan_.kind = PlanKind::GROUP_REDUCE;
+        const int T = plan_.threads;
+        const int G = (int)groups.size(), M = (int)groups[0].size();
+        plan_.groups = G;
+        plan_.aggs = M;
+        const auto& g0 = groups[0];
+        std::ostringstream o;
+        o << "#define RF_G " << G << "\n#define RF_M " << M << "\n\n";
+        // per-aggregate value struct
+        o << "struct RfVals {\n";
+        for (int m = 0; m < M; m++) {
+            auto& lf = leaves[g0[m]];
+            std::string ct = lf.count ? "long long" : (lf.op == AggOp::OR || lf.op == AggOp::AND) ? "long long" : ctype(lf.type);
+            o << "    " << ct << " v" << m << ";\n";
+        }
+        o << "};\n\n";
+        // 64-bit slot encode/decode per aggregate
+        auto enc = [&](const Leaf& lf, const std::string& x) -> std::string {
+            if (!lf.count && lf.type.is_float()) return "rf_f2u((double)(" + x + "))";
+            return "(unsigned long long)(long long)(" + x + ")";
+        };
+        auto dec = [&](const Leaf& lf, const std::string& x) -> std::string {
+            if (!lf.count && lf.type.is_float()) return "rf_u2f(" + x + ")";
+            if (lf.type.is_unsigned()) return "(unsigned long long)(" + x + ")";
+            return "(long long)(" + x + ")";
+        };
+        // slot identity (sums: 0; idempotent ops: the leaf's init, per aggregate index m; the
+        // init must then agree across groups, which holds for the shapes detect_groups admits
+        // only when it is the same expression - checked here)
+        Emitter Ei(*this);
+        bind_inputs(Ei);
+        std::ostringstream initsw;
+        for (int m = 0; m < M; m++) {
+            auto& lf = leaves[g0[m]];
+            std::string v = lf.op == AggOp::SUM ? "0ULL" : enc(lf, "(" + acc_ctype(lf) + ")(" + Ei.ev(lf.init).c + ")");
+            if (lf.op != AggOp::SUM)
+                for (int g = 1; g < G; g++)
+                    if (!same(leaves[groups[g][m]].init, lf.init)) throw LowerError("grouped min/max with differing inits");
+            initsw << "        case " << m << ": return " << v << ";\n";
+        }
+        o << "RF_DEV unsigned long long rf_slot_init(const RfParams& P, int m)\n{\n";
+        for (auto& dcl : Ei.decls) o << "    " << dcl << "\n";
+        o << "    switch (m) {\n" << initsw.str() << "        default: return 0ULL;\n    }\n}\n\n";
+        o << "RF_DEV unsigned long long rf_slot_combine(int m, unsigned long long a, unsigned long long b)\n{\n    switch (m) {\n";
+        for (int m = 0; m < M; m++) {
+            auto& lf = leaves[g0[m]];
+            std::string ct = lf.count ? "long long" : (lf.op == AggOp::OR || lf.op == AggOp::AND) ? "long long" : ctype(lf.type);
+            std::string A = "(" + ct + ")" + dec(lf, "a"), B = "(" + ct + ")" + dec(lf, "b");
+            std::string e = combine_expr(lf, A, B);
+            o << "        case " << m << ": return " << enc(lf, e) << ";\n";
+        }
+        o << "        default: return a;\n    }\n}\n\n";
+        o << "RF_DEV void rf_slot_add(unsigned long long* S, int g, int t, const RfVals& V)\n{\n";
+        for (int m = 0; m < M; m++) {
+            o << "    { unsigned long long* s = S + (g * RF_M + " << m << ") * " << T << " + t; *s = rf_slot_combine("
+              << m << ", *s, ";
+            auto& lf = leaves[g0[m]];
+            o << enc(lf, "V.v" + std::to_string(m)) << "); }\n";
+        }
+        o << "}\n\n";
+
+        // group function
+        Emitter E(*this);
+        std::ostringstream body;
+        std::string rowcond = bind_row(E, red, d, body);
+        std::ostringstream gb;
+        std::string filt = "true";
+        if (!filters.empty()) {
+            Expr f = filters[0];
+            for (size_t i = 1; i < filters.size(); i++) f = reffiner::_and(f, filters[i]);
+            filt = E.ev(order_conjuncts(f)).c;
+        }
+        gb << "    if (!(" << filt << ")) return -1;\n";
+        for (size_t k = 0; k < key_exprs.size(); k++) gb << "    const auto key" << k << " = " << E.ev(key_exprs[k]).c << ";\n";
+        gb << "    int g = -1;\n";
+        for (int g = 0; g < G; g++) {
+            auto& lf = leaves[groups[g][0]];
+            gb << "    " << (g ? "else if (" : "if (");
+            for (size_t k = 0; k < key_exprs.size(); k++) {
+                if (k) gb << " && ";
+                gb << "(key" << k << " == " << E.ev(lf.keys[k].second).c << ")";
+            }
+            gb << ") g = " << g << ";\n";
+        }
+        gb << "    if (g < 0) return -1;\n";
+        for (int m = 0; m < M; m++) {
+            auto& lf = leaves[g0[m]];
+            std::string val;
+            if (lf.count) val = "1";
+            else if (lf.op == AggOp::OR || lf.op == AggOp::AND) val = "(long long)(" + E.ev(lf.value).c + ")";
+            else val = "(" + ctype(lf.type) + ")(" + E.ev(lf.value).c + ")";
+            gb << "    V.v" << m << " = " << val << ";\n";
+        }
+        gb << "    return g;\n";
+        o << "RF_DEV int rf_group(const RfParams& P, long long r, RfVals& V)\n{\n";
+        o << body.str();
+        for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+        o << "    if (!(" << rowcond << ")) return -1;\n";
+        o << gb.str() << "}\n\n";
+
+        // epilogue
+        Emitter Ef(*this);
+        bind_inputs(Ef);
+        std::map<std::vector<size_t>, std::string> finals;
+        std::ostringstream fb;
+        std::map<int, std::pair<int, int>> leaf_gm;
+        for (int g = 0; g < G; g++)
+            for (int m = 0; m < M; m++) leaf_gm[groups[g][m]] = {g, m};
+        for (size_t i = 0; i < leaves.size(); i++) {
+            auto& lf = leaves[i];
+            std::string tot = "0";
+            if (lf.op != AggOp::NONE) {
+                auto gm = leaf_gm.at((int)i);
+                tot = dec(lf, "S[" + std::to_string(gm.first * M + gm.second) + "]");
+            }
+            std::string nm = "st" + std::to_string(i);
+            fb << "    const " << ctype(lf.type) << " " << nm << " = " << final_leaf(Ef, lf, tot) << ";\n";
+            finals[lf.path] = nm;
+        }
+        std::ostringstream stores;
+        emit_output_store(Ef, stores, red, finals);
+        o << "RF_DEV void rf_finish_groups(const RfParams& P, const unsigned long long* S, unsigned char* out)\n{\n";
+        for (auto& dcl : Ef.decls) o << "    " << dcl << "\n";
+        o << fb.str() << stores.str() << "}\n\n";
+
+        src << o.str();
+        src << "#define RF_GROUP_REDUCE 1\n#include \"rf_templates.cuh\"\n";
+        src << "RF_GROUP_REDUCE_KERNEL(rf_main, " << T << ")\n";
+        size_t smem = (size_t)G * M * T * 8;
+        if (smem > 200 * 1024) throw LowerError("too many group accumulators for shared memory");
+        plan_.kernels.push_back({"rf_main", T, smem, KernelSpec::MAIN});
+        plan_.acc_bytes = (size_t)G * M * 8;
+    }
+
+    // ---------------------------------------------------------------- Op lowering (tables)
+    void lower_op(const Expr& opx)
+    {
+        (void)opx;
+        throw LowerError("Op outputs are lowered by the materialisation templates (not yet available)");
+    }
+
+    std::shared_ptr<Func> fn_;
+    bool vectorize_;
+    Plan plan_;
+    std::map<const ExprNode*, int> input_index_;
+};
+
+}  // namespace
+
+size_t c_align(const DataType& t)
+{
+    if (t.is_struct()) {
+        size_t a = 1;
+        for (auto& d : t.dtypes) a = std::max(a, c_align(d));
+        return a;
+    }
+    return t.size();
+}
+
+size_t c_size(const DataType& t)
+{
+    if (t.is_struct()) {
+        size_t off = 0;
+        for (auto& d : t.dtypes) {
+            size_t al = c_align(d);
+            off = (off + al - 1) / al * al + c_size(d);
+        }
+        size_t al = c_align(t);
+        return (off + al - 1) / al * al;
+    }
+    return t.size();
+}
+
+Plan lower(const std::shared_ptr<Func>& fn, bool vectorize) { return Lowerer(fn, vectorize).run(); }
+
+}  // namespace rfg

@@ -1,0 +1,1062 @@
+// C-ABI runtime of the GB300 backend (include/rf_gpu.h).
+//
+// Replaces, for the compiled-query path, Reffine's ExecEngine/CudaEngine (src/engine/*.cpp):
+// a query is lowered (lower.cpp), its CUDA source compiled by NVRTC for sm_103a and loaded
+// through the driver API; tables live in device memory; runs are stream-ordered.
+#include <cuda.h>
+#include <cuda_runtime_api.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "arrow_c.h"
+#include "device/rf_params.h"
+#include "kernels.h"
+#include "lower.h"
+#include "rf_gpu.h"
+#include "runtime.h"
+
+namespace {
+
+const char* k_device_src =
+#include "rf_device.cuh.inc"
+    ;
+const char* k_templates_src =
+#include "rf_templates.cuh.inc"
+    ;
+const char* k_params_src =
+#include "rf_params.h.inc"
+    ;
+
+// ------------------------------------------------------------------------------------------
+// driver API entry points (resolved through the runtime, so the library does not link libcuda)
+// ------------------------------------------------------------------------------------------
+struct Driver {
+    CUresult (*ModuleLoadData)(CUmodule*, const void*) = nullptr;
+    CUresult (*ModuleUnload)(CUmodule) = nullptr;
+    CUresult (*ModuleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+    CUresult (*LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                             CUstream, void**, void**) = nullptr;
+    CUresult (*FuncSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
+    CUresult (*GetErrorString)(CUresult, const char**) = nullptr;
+    bool ok = false;
+    std::string err;
+};
+
+Driver& drv()
+{
+    static Driver d;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        auto get = [&](const char* name, void** fn) -> bool {
+            cudaDriverEntryPointQueryResult q;
+            cudaError_t e = cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q);
+            if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !*fn) {
+                d.err = std::string("driver entry point unavailable: ") + name;
+                return false;
+            }
+            return true;
+        };
+        d.ok = get("cuModuleLoadData", (void**)&d.ModuleLoadData) && get("cuModuleUnload", (void**)&d.ModuleUnload) &&
+               get("cuModuleGetFunction", (void**)&d.ModuleGetFunction) &&
+               get("cuLaunchKernel", (void**)&d.LaunchKernel) && get("cuFuncSetAttribute", (void**)&d.FuncSetAttribute) &&
+               get("cuOccupancyMaxActiveBlocksPerMultiprocessor", (void**)&d.OccupancyMaxActiveBlocksPerMultiprocessor) &&
+               get("cuGetErrorString", (void**)&d.GetErrorString);
+    });
+    return d;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// objects
+// ------------------------------------------------------------------------------------------
+struct JitModule {
+    CUmodule mod = nullptr;
+    std::map<std::string, CUfunction> fns;
+    std::string log;
+    ~JitModule()
+    {
+        if (mod && drv().ok) drv().ModuleUnload(mod);
+    }
+};
+
+struct rf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::string err;
+    std::map<std::string, std::shared_ptr<JitModule>> modules;
+    std::atomic<long long> launches{0};
+    int sm_count = 0;
+    int* dev_err = nullptr;  // device error word shared by this context's launches
+};
+
+struct DevCol {
+    reffine::DataType type;
+    bool runend = false;
+    void* data = nullptr;             // values (run values)
+    long long nvals = 0;
+    unsigned short* valid = nullptr;  // validity of the values (NULL: all valid)
+    int* run_ends = nullptr;
+    long long logical = 0;            // rows
+    std::string name;
+    // allocations behind the pointers above (reused by repeated uploads into the same table)
+    void* data_buf = nullptr;
+    void* valid_buf = nullptr;
+    void* re_buf = nullptr;
+    size_t data_cap = 0, valid_cap = 0, re_cap = 0;
+};
+
+struct rf_table {
+    rf_ctx* ctx = nullptr;
+    long long dim = 1;
+    std::vector<DevCol> cols;
+    std::vector<char> present;        // column uploaded
+    long long* ix_slots = nullptr;
+    unsigned long long ix_cap = 0;
+    long long* ix_special = nullptr;
+    bool has_index = false;
+    long long null_count = 0;
+    std::string name;
+};
+
+struct rf_plan {
+    rf_ctx* ctx = nullptr;
+    std::vector<rf_table*> staging;   // device copies of the host tables of thunk calls
+    rfg::Plan plan;
+    std::shared_ptr<JitModule> mod;
+    std::vector<CUfunction> fns;
+    void* partials = nullptr;
+    size_t partials_bytes = 0;
+    unsigned* counter = nullptr;
+    long long* range = nullptr;
+    unsigned char* dout = nullptr;
+    int max_units = 0;
+    int thunk_slot = -1;
+    std::vector<std::unique_ptr<rf_table>> thunk_outputs;
+};
+
+// ------------------------------------------------------------------------------------------
+// helpers
+// ------------------------------------------------------------------------------------------
+namespace {
+
+int fail(rf_ctx* ctx, int code, const char* fmt, ...)
+{
+    char buf[4096];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->err = buf;
+    return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                      \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail(ctx, RF_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
+    } while (0)
+
+int cu_fail(rf_ctx* ctx, CUresult r, const char* what)
+{
+    const char* s = "?";
+    if (drv().GetErrorString) drv().GetErrorString(r, &s);
+    return fail(ctx, RF_ERR_CUDA, "%s failed: %s", what, s);
+}
+
+bool parse_format(const char* f, reffine::DataType& t)
+{
+    using namespace reffine;
+    std::string s(f ? f : "");
+    if (s == "c") t = DataType(INT8);
+    else if (s == "C") t = DataType(UINT8);
+    else if (s == "s") t = DataType(INT16);
+    else if (s == "S") t = DataType(UINT16);
+    else if (s == "i") t = DataType(INT32);
+    else if (s == "I") t = DataType(UINT32);
+    else if (s == "l") t = DataType(INT64);
+    else if (s == "L") t = DataType(UINT64);
+    else if (s == "f") t = DataType(FLOAT32);
+    else if (s == "g") t = DataType(FLOAT64);
+    else return false;
+    return true;
+}
+
+const char* format_of(const reffine::DataType& t)
+{
+    using namespace reffine;
+    switch (t.btype) {
+        case BOOL: case INT8: return "c";
+        case UINT8: return "C";
+        case INT16: return "s";
+        case UINT16: return "S";
+        case INT32: return "i";
+        case UINT32: return "I";
+        case INT64: case IDX: return "l";
+        case UINT64: return "L";
+        case FLOAT32: return "f";
+        case FLOAT64: return "g";
+        default: return "?";
+    }
+}
+
+long long eval_host(const rfg::HostExpr& h, const rf_arg* args, int n_args, bool& ok)
+{
+    switch (h.kind) {
+        case rfg::HostExpr::CONST: return h.value;
+        case rfg::HostExpr::LEN: {
+            if (h.input >= n_args || args[h.input].kind != RF_ARG_TABLE || !args[h.input].table) {
+                ok = false;
+                return 0;
+            }
+            auto* t = args[h.input].table;
+            if (h.col >= (int)t->cols.size()) {
+                ok = false;
+                return 0;
+            }
+            return t->cols[h.col].nvals;
+        }
+        case rfg::HostExpr::SCALAR:
+            if (h.input >= n_args) {
+                ok = false;
+                return 0;
+            }
+            return args[h.input].kind == RF_ARG_F64 ? (long long)args[h.input].f64 : args[h.input].i64;
+        case rfg::HostExpr::ADD: return eval_host(h.args[0], args, n_args, ok) + eval_host(h.args[1], args, n_args, ok);
+        case rfg::HostExpr::SUB: return eval_host(h.args[0], args, n_args, ok) - eval_host(h.args[1], args, n_args, ok);
+        case rfg::HostExpr::MUL: return eval_host(h.args[0], args, n_args, ok) * eval_host(h.args[1], args, n_args, ok);
+        case rfg::HostExpr::MAX: {
+            long long a = eval_host(h.args[0], args, n_args, ok), b = eval_host(h.args[1], args, n_args, ok);
+            return a > b ? a : b;
+        }
+        case rfg::HostExpr::MIN: {
+            long long a = eval_host(h.args[0], args, n_args, ok), b = eval_host(h.args[1], args, n_args, ok);
+            return a < b ? a : b;
+        }
+        default: ok = false; return 0;
+    }
+}
+
+std::string nvrtc_arch()
+{
+    const char* a = getenv("RF_GPU_ARCH");
+    return std::string("--gpu-architecture=") + (a && *a ? a : "sm_103a");
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// JIT
+// ------------------------------------------------------------------------------------------
+namespace rfrt {
+
+// compiles a generated query source for sm_103a; on failure `log` holds the message
+bool nvrtc_compile(const std::string& src, std::string& cubin, std::string& log)
+{
+    nvrtcProgram prog;
+    const char* hdrs[] = {k_device_src, k_templates_src, k_params_src};
+    const char* names[] = {"rf_device.cuh", "rf_templates.cuh", "rf_params.h"};
+    if (nvrtcCreateProgram(&prog, src.c_str(), "query.cu", 3, hdrs, names) != NVRTC_SUCCESS) {
+        log = "nvrtcCreateProgram failed";
+        return false;
+    }
+    std::string arch = nvrtc_arch();
+    // --fmad=false: products are rounded before sums, as the reference's C++ does with
+    // -ffp-contract=off; results then match the serial CPU loop per row
+    const char* opts[] = {arch.c_str(), "-std=c++17", "--fmad=false", "-lineinfo"};
+    nvrtcResult r = nvrtcCompileProgram(prog, 4, opts);
+    size_t lsz = 0;
+    nvrtcGetProgramLogSize(prog, &lsz);
+    std::string l(lsz, '\0');
+    if (lsz) nvrtcGetProgramLog(prog, &l[0]);
+    if (r != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        log = std::string("NVRTC compile failed: ") + nvrtcGetErrorString(r) + "\n" + l + "\n--- source ---\n" + src;
+        return false;
+    }
+    size_t csz = 0;
+    nvrtcGetCUBINSize(prog, &csz);
+    cubin.assign(csz, '\0');
+    nvrtcGetCUBIN(prog, &cubin[0]);
+    nvrtcDestroyProgram(&prog);
+    log = l;
+    return true;
+}
+
+int jit_compile(rf_ctx* ctx, const std::string& key, const std::string& src, std::shared_ptr<JitModule>& out,
+                std::string* cubin_out)
+{
+    {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        auto it = ctx->modules.find(key);
+        if (it != ctx->modules.end()) {
+            out = it->second;
+            return RF_OK;
+        }
+    }
+    std::string cubin, log;
+    if (!nvrtc_compile(src, cubin, log)) return fail(ctx, RF_ERR_JIT, "%s", log.c_str());
+    if (cubin_out) *cubin_out = cubin;
+    auto m = std::make_shared<JitModule>();
+    m->log = log;
+    if (!drv().ok) return fail(ctx, RF_ERR_CUDA, "%s", drv().err.c_str());
+    CUresult cr = drv().ModuleLoadData(&m->mod, cubin.data());
+    if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "cuModuleLoadData");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->modules[key] = m;
+    out = m;
+    return RF_OK;
+}
+
+int get_function(rf_ctx* ctx, JitModule& m, const std::string& name, CUfunction& f)
+{
+    auto it = m.fns.find(name);
+    if (it != m.fns.end()) {
+        f = it->second;
+        return RF_OK;
+    }
+    CUresult cr = drv().ModuleGetFunction(&f, m.mod, name.c_str());
+    if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "cuModuleGetFunction");
+    m.fns[name] = f;
+    return RF_OK;
+}
+
+int launch(rf_ctx* ctx, CUfunction f, int grid, int block, size_t smem, cudaStream_t s, RfParams* P)
+{
+    void* args[] = {P};
+    CUresult cr = drv().LaunchKernel(f, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)s, args, nullptr);
+    if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "cuLaunchKernel");
+    ctx->launches++;
+    return RF_OK;
+}
+
+}  // namespace rfrt
+
+using namespace rfrt;
+
+// ------------------------------------------------------------------------------------------
+// context
+// ------------------------------------------------------------------------------------------
+extern "C" int rf_gpu_init(int device, rf_ctx** out)
+{
+    if (!out) return RF_ERR_INVALID;
+    *out = nullptr;
+    auto ctx = std::make_unique<rf_ctx>();
+    ctx->device = device;
+    CUDA_TRY(nullptr, cudaSetDevice(device));
+    CUDA_TRY(nullptr, cudaFree(nullptr));
+    if (!drv().ok) return RF_ERR_CUDA;
+    CUDA_TRY(nullptr, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CUDA_TRY(nullptr, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
+    CUDA_TRY(nullptr, cudaMalloc((void**)&ctx->dev_err, sizeof(int)));
+    CUDA_TRY(nullptr, cudaMemset(ctx->dev_err, 0, sizeof(int)));
+    *out = ctx.release();
+    return RF_OK;
+}
+
+extern "C" int rf_gpu_shutdown(rf_ctx* ctx)
+{
+    if (!ctx) return RF_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->modules.clear();
+    cudaFree(ctx->dev_err);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return RF_OK;
+}
+
+extern "C" const char* rf_last_error(rf_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+extern "C" int rf_ctx_stream(rf_ctx* ctx, void** stream)
+{
+    if (!ctx || !stream) return RF_ERR_INVALID;
+    *stream = ctx->stream;
+    return RF_OK;
+}
+
+namespace {
+int check_device_error(rf_ctx* ctx)
+{
+    int e = 0;
+    CUDA_TRY(ctx, cudaMemcpy(&e, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        cudaMemset(ctx->dev_err, 0, sizeof(int));
+        const char* what = e == RF_DEVERR_PROBE ? "hash probe exhausted the table"
+                           : e == RF_DEVERR_WAIT ? "bounded wait ran out"
+                           : e == RF_DEVERR_RANGE ? "loop lower bound not found in the iterator column (Locate returned -1)"
+                           : e == RF_DEVERR_OVERFLOW ? "output capacity exceeded"
+                                                     : "unknown device error";
+        return fail(ctx, RF_ERR_DEVICE, "device error %d: %s", e, what);
+    }
+    return RF_OK;
+}
+}  // namespace
+
+extern "C" int rf_ctx_sync(rf_ctx* ctx)
+{
+    if (!ctx) return RF_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return check_device_error(ctx);
+}
+
+extern "C" int rf_ctx_launch_count(rf_ctx* ctx, int64_t* count)
+{
+    if (!ctx || !count) return RF_ERR_INVALID;
+    *count = ctx->launches.load();
+    return RF_OK;
+}
+
+extern "C" int rf_host_alloc(rf_ctx* ctx, size_t bytes, void** ptr)
+{
+    if (!ctx || !ptr) return RF_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    if (cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess)
+        return fail(ctx, RF_ERR_OOM, "cudaHostAlloc(%zu) failed", bytes);
+    return RF_OK;
+}
+
+extern "C" int rf_host_free(rf_ctx* ctx, void* ptr)
+{
+    if (!ctx) return RF_ERR_INVALID;
+    if (ptr) cudaFreeHost(ptr);
+    return RF_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// tables
+// ------------------------------------------------------------------------------------------
+namespace {
+
+// copies `bytes` from host `src` into the allocation (*buf, *cap), growing it if needed;
+// *active is set to the copy, or NULL when there is nothing to copy
+int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src, size_t bytes, cudaStream_t s)
+{
+    *active = nullptr;
+    if (!src || bytes == 0) return RF_OK;
+    if (!*buf || *cap < bytes) {
+        if (*buf) {
+            cudaStreamSynchronize(s);
+            cudaFree(*buf);
+        }
+        *buf = nullptr;
+        *cap = 0;
+        // 16 bytes of slack: vector loads may touch the tail of the last element's 16-byte line
+        if (cudaMalloc(buf, bytes + 16) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "cudaMalloc(%zu) failed", bytes);
+        *cap = bytes;
+    }
+    CUDA_TRY(ctx, cudaMemcpyAsync(*buf, src, bytes, cudaMemcpyHostToDevice, s));
+    *active = *buf;
+    return RF_OK;
+}
+
+void free_table_mem(rf_table* t)
+{
+    for (auto& c : t->cols) {
+        cudaFree(c.data_buf);
+        cudaFree(c.valid_buf);
+        cudaFree(c.re_buf);
+    }
+    cudaFree(t->ix_slots);
+    cudaFree(t->ix_special);
+}
+
+}  // namespace
+
+namespace rfrt {
+
+int upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int64_t dim, const int32_t* sel, int32_t nsel,
+           void* stream, rf_table** out, rf_table* reuse)
+{
+    if (!ctx || !schema || !array || !out) return fail(ctx, RF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    if (!schema->format || std::string(schema->format) != "+s")
+        return fail(ctx, RF_ERR_INVALID, "table schema must be a struct (+s), got %s", schema->format ? schema->format : "null");
+    if (schema->n_children != array->n_children) return fail(ctx, RF_ERR_INVALID, "schema/array child count mismatch");
+    if (array->offset != 0) return fail(ctx, RF_ERR_UNSUPPORTED, "arrays with an offset are not supported");
+    long long n = schema->n_children;
+    if (n > RF_MAX_COLS) return fail(ctx, RF_ERR_UNSUPPORTED, "table has %lld columns (max %d)", n, RF_MAX_COLS);
+    std::unique_ptr<rf_table> owned;
+    rf_table* t = reuse;
+    if (t && (long long)t->cols.size() != n) {
+        free_table_mem(t);
+        t->cols.clear();
+    }
+    if (!t) {
+        owned = std::make_unique<rf_table>();
+        t = owned.get();
+    }
+    t->ctx = ctx;
+    t->dim = dim;
+    t->name = schema->name ? schema->name : "";
+    t->has_index = false;
+    t->null_count = 0;
+    t->cols.resize(n);
+    t->present.assign(n, 0);
+    std::vector<char> want(n, sel ? 0 : 1);
+    for (int i = 0; sel && i < nsel; i++)
+        if (sel[i] >= 0 && sel[i] < n) want[sel[i]] = 1;
+    for (long long c = 0; c < n; c++) {
+        const ArrowSchema* cs = schema->children[c];
+        const ArrowArray* ca = array->children[c];
+        DevCol& dc = t->cols[c];
+        dc.name = cs->name ? cs->name : "";
+        if (ca->offset != 0) return fail(ctx, RF_ERR_UNSUPPORTED, "column %lld has an offset", c);
+        std::string fmt = cs->format ? cs->format : "";
+        if (fmt == "+r") {
+            if (cs->n_children != 2 || ca->n_children != 2)
+                return fail(ctx, RF_ERR_INVALID, "run-end column %lld needs 2 children", c);
+            const ArrowArray* re = ca->children[0];
+            const ArrowArray* va = ca->children[1];
+            if (std::string(cs->children[0]->format) != "i")
+                return fail(ctx, RF_ERR_UNSUPPORTED, "run ends must be int32 (column %lld)", c);
+            if (!parse_format(cs->children[1]->format, dc.type))
+                return fail(ctx, RF_ERR_UNSUPPORTED, "column %lld: format %s", c, cs->children[1]->format);
+            dc.runend = true;
+            dc.nvals = va->length;
+            dc.logical = ca->length;
+            if (re->length != va->length) return fail(ctx, RF_ERR_INVALID, "run ends and values differ in length");
+            dc.data = nullptr;
+            dc.valid = nullptr;
+            dc.run_ends = nullptr;
+            if (want[c]) {
+                int rc;
+                if ((rc = copy_in(ctx, (void**)&dc.run_ends, &dc.re_buf, &dc.re_cap, re->buffers[1], re->length * 4, s)))
+                    return rc;
+                if ((rc = copy_in(ctx, &dc.data, &dc.data_buf, &dc.data_cap, va->buffers[1], va->length * dc.type.size(), s)))
+                    return rc;
+                if (va->n_buffers > 0 && va->buffers[0] && va->null_count != 0)
+                    if ((rc = copy_in(ctx, (void**)&dc.valid, &dc.valid_buf, &dc.valid_cap, va->buffers[0],
+                                      ((va->length + 15) / 16) * 2, s)))
+                        return rc;
+            }
+        } else {
+            if (!parse_format(cs->format, dc.type)) return fail(ctx, RF_ERR_UNSUPPORTED, "column %lld: format %s", c, cs->format);
+            dc.runend = false;
+            dc.nvals = ca->length;
+            dc.logical = ca->length;
+            dc.data = nullptr;
+            dc.valid = nullptr;
+            dc.run_ends = nullptr;
+            if (want[c]) {
+                int rc;
+                if (ca->n_buffers < 2) return fail(ctx, RF_ERR_INVALID, "column %lld has no value buffer", c);
+                if ((rc = copy_in(ctx, &dc.data, &dc.data_buf, &dc.data_cap, ca->buffers[1], ca->length * dc.type.size(), s)))
+                    return rc;
+                if (ca->buffers[0] && ca->null_count != 0)
+                    if ((rc = copy_in(ctx, (void**)&dc.valid, &dc.valid_buf, &dc.valid_cap, ca->buffers[0],
+                                      ((ca->length + 15) / 16) * 2, s)))
+                        return rc;
+            }
+        }
+        t->present[c] = want[c];
+    }
+    if (owned) owned.release();
+    *out = t;
+    return RF_OK;
+}
+
+int build_index(rf_table* t, cudaStream_t s)
+{
+    rf_ctx* ctx = t->ctx;
+    if (t->cols.empty()) return fail(ctx, RF_ERR_INVALID, "empty table");
+    DevCol& c0 = t->cols[0];
+    if (c0.type.btype != reffine::INT64)
+        return fail(ctx, RF_ERR_UNSUPPORTED, "Data type not supported for indexing: %s", c0.type.str().c_str());
+    if (!t->present[0]) return fail(ctx, RF_ERR_INVALID, "column 0 not on the device");
+    unsigned long long cap = (unsigned long long)(2 * c0.nvals);  // load factor 0.5
+    if (cap < 2) cap = 2;
+    cudaFree(t->ix_slots);
+    cudaFree(t->ix_special);
+    t->ix_slots = nullptr;
+    t->ix_special = nullptr;
+    if (cudaMalloc((void**)&t->ix_slots, cap * 16) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
+    if (cudaMalloc((void**)&t->ix_special, 8) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
+    t->ix_cap = cap;
+    int e = rf_k_index_build(c0.data, c0.valid, c0.nvals, t->ix_slots, cap, t->ix_special, ctx->dev_err, s);
+    if (e) return fail(ctx, RF_ERR_CUDA, "index build launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    ctx->launches += c0.nvals > 0 ? 2 : 1;
+    t->has_index = true;
+    return RF_OK;
+}
+
+}  // namespace rfrt
+
+extern "C" int rf_table_upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int64_t dim,
+                               void* stream, rf_table** out)
+{
+    return upload(ctx, schema, array, dim, nullptr, 0, stream, out, nullptr);
+}
+
+extern "C" int rf_table_upload_cols(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int64_t dim,
+                                    const int32_t* cols, int32_t n_cols, void* stream, rf_table** out)
+{
+    return upload(ctx, schema, array, dim, cols, n_cols, stream, out, nullptr);
+}
+
+extern "C" int rf_table_free(rf_table* t)
+{
+    if (!t) return RF_OK;
+    cudaSetDevice(t->ctx->device);
+    cudaStreamSynchronize(t->ctx->stream);
+    free_table_mem(t);
+    delete t;
+    return RF_OK;
+}
+
+extern "C" int rf_table_build_index(rf_table* t, void* stream)
+{
+    if (!t) return RF_ERR_INVALID;
+    cudaSetDevice(t->ctx->device);
+    return build_index(t, stream ? (cudaStream_t)stream : t->ctx->stream);
+}
+
+extern "C" int rf_table_num_rows(rf_table* t, int64_t* rows)
+{
+    if (!t || !rows) return RF_ERR_INVALID;
+    *rows = t->cols.empty() ? 0 : t->cols[0].logical;
+    return RF_OK;
+}
+
+extern "C" int rf_table_num_cols(rf_table* t, int32_t* cols)
+{
+    if (!t || !cols) return RF_ERR_INVALID;
+    *cols = (int32_t)t->cols.size();
+    return RF_OK;
+}
+
+extern "C" int rf_table_null_count(rf_table* t, int64_t* nulls)
+{
+    if (!t || !nulls) return RF_ERR_INVALID;
+    *nulls = t->null_count;
+    return RF_OK;
+}
+
+extern "C" int rf_table_column(rf_table* t, int32_t col, int32_t part, void** dev_ptr, int64_t* count)
+{
+    if (!t || !dev_ptr || col < 0 || col >= (int32_t)t->cols.size()) return RF_ERR_INVALID;
+    auto& c = t->cols[col];
+    if (part == 0) {
+        *dev_ptr = c.data;
+        if (count) *count = c.nvals;
+    } else if (part == 1) {
+        *dev_ptr = c.valid;
+        if (count) *count = c.valid ? (c.nvals + 15) / 16 * 2 : 0;
+    } else if (part == 2) {
+        *dev_ptr = c.run_ends;
+        if (count) *count = c.runend ? c.nvals : 0;
+    } else {
+        return RF_ERR_INVALID;
+    }
+    return RF_OK;
+}
+
+// ---- export: device table -> host Arrow C data (owned; released through callbacks) --------
+namespace {
+
+struct ExportSchemaPriv {
+    std::string format, name;
+    std::vector<ArrowSchema*> children;
+    std::vector<ArrowSchema> child_store;
+};
+struct ExportArrayPriv {
+    std::vector<void*> bufs;       // malloc'ed
+    std::vector<const void*> buf_ptrs;
+    std::vector<ArrowArray*> children;
+    std::vector<ArrowArray> child_store;
+};
+
+void release_schema(ArrowSchema* s)
+{
+    if (!s || !s->release) return;
+    auto* p = (ExportSchemaPriv*)s->private_data;
+    if (p) {
+        for (auto& c : p->child_store)
+            if (c.release) c.release(&c);
+        delete p;
+    }
+    s->release = nullptr;
+}
+
+void release_array(ArrowArray* a)
+{
+    if (!a || !a->release) return;
+    auto* p = (ExportArrayPriv*)a->private_data;
+    if (p) {
+        for (auto& c : p->child_store)
+            if (c.release) c.release(&c);
+        for (void* b : p->bufs) free(b);
+        delete p;
+    }
+    a->release = nullptr;
+}
+
+void init_schema(ArrowSchema* s, const std::string& fmt, const std::string& name, size_t nchildren)
+{
+    auto* p = new ExportSchemaPriv();
+    p->format = fmt;
+    p->name = name;
+    p->child_store.resize(nchildren);
+    p->children.resize(nchildren);
+    for (size_t i = 0; i < nchildren; i++) p->children[i] = &p->child_store[i];
+    memset(s, 0, sizeof(*s));
+    s->format = p->format.c_str();
+    s->name = p->name.c_str();
+    s->flags = ARROW_FLAG_NULLABLE;
+    s->n_children = (int64_t)nchildren;
+    s->children = nchildren ? p->children.data() : nullptr;
+    s->release = release_schema;
+    s->private_data = p;
+}
+
+ExportArrayPriv* init_array(ArrowArray* a, long long length, long long nulls, size_t nbuffers, size_t nchildren)
+{
+    auto* p = new ExportArrayPriv();
+    p->buf_ptrs.assign(nbuffers, nullptr);
+    p->child_store.resize(nchildren);
+    p->children.resize(nchildren);
+    for (size_t i = 0; i < nchildren; i++) p->children[i] = &p->child_store[i];
+    memset(a, 0, sizeof(*a));
+    a->length = length;
+    a->null_count = nulls;
+    a->n_buffers = (int64_t)nbuffers;
+    a->n_children = (int64_t)nchildren;
+    a->buffers = nbuffers ? p->buf_ptrs.data() : nullptr;
+    a->children = nchildren ? p->children.data() : nullptr;
+    a->release = release_array;
+    a->private_data = p;
+    return p;
+}
+
+int fetch(rf_ctx* ctx, ExportArrayPriv* p, int slot, const void* dsrc, size_t bytes)
+{
+    if (!dsrc || bytes == 0) return RF_OK;
+    void* h = malloc(bytes);
+    if (!h) return fail(ctx, RF_ERR_OOM, "host allocation failed");
+    p->bufs.push_back(h);
+    CUDA_TRY(ctx, cudaMemcpy(h, dsrc, bytes, cudaMemcpyDeviceToHost));
+    p->buf_ptrs[slot] = h;
+    return RF_OK;
+}
+
+}  // namespace
+
+extern "C" int rf_table_export(rf_table* t, ArrowSchema* so, ArrowArray* ao)
+{
+    if (!t || !so || !ao) return RF_ERR_INVALID;
+    rf_ctx* ctx = t->ctx;
+    cudaSetDevice(ctx->device);
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    size_t n = t->cols.size();
+    long long rows = n ? t->cols[0].logical : 0;
+    init_schema(so, "+s", t->name, n);
+    auto* ap = init_array(ao, rows, 0, 1, n);
+    for (size_t c = 0; c < n; c++) {
+        auto& dc = t->cols[c];
+        auto* sp = (ExportSchemaPriv*)so->private_data;
+        ArrowSchema* cs = sp->children[c];
+        ArrowArray* ca = ap->children[c];
+        long long nulls = dc.valid ? t->null_count : 0;
+        if (dc.runend) {
+            init_schema(cs, "+r", dc.name, 2);
+            auto* csp = (ExportSchemaPriv*)cs->private_data;
+            init_schema(csp->children[0], "i", "run_ends", 0);
+            init_schema(csp->children[1], format_of(dc.type), "values", 0);
+            auto* cap = init_array(ca, dc.logical, 0, 0, 2);
+            auto* rp = init_array(cap->children[0], dc.nvals, 0, 2, 0);
+            auto* vp = init_array(cap->children[1], dc.nvals, nulls, 2, 0);
+            int rc;
+            if ((rc = fetch(ctx, rp, 1, dc.run_ends, dc.nvals * 4))) return rc;
+            if ((rc = fetch(ctx, vp, 1, dc.data, dc.nvals * dc.type.size()))) return rc;
+            if ((rc = fetch(ctx, vp, 0, dc.valid, (dc.nvals + 15) / 16 * 2))) return rc;
+        } else {
+            init_schema(cs, format_of(dc.type), dc.name, 0);
+            auto* cp = init_array(ca, dc.nvals, nulls, 2, 0);
+            int rc;
+            if ((rc = fetch(ctx, cp, 1, dc.data, dc.nvals * dc.type.size()))) return rc;
+            if ((rc = fetch(ctx, cp, 0, dc.valid, (dc.nvals + 15) / 16 * 2))) return rc;
+        }
+    }
+    return RF_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// plans
+// ------------------------------------------------------------------------------------------
+extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_plan** out)
+{
+    if (!ctx || !text || !out) return fail(ctx, RF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    auto p = std::make_unique<rf_plan>();
+    p->ctx = ctx;
+    try {
+        auto fn = reffine::parse_text(text);
+        p->plan = rfg::lower(fn, vectorize != 0);
+    } catch (const rfg::LowerError& e) {
+        return fail(ctx, e.unsupported ? RF_ERR_UNSUPPORTED : RF_ERR_INVALID, "%s", e.what());
+    } catch (const std::exception& e) {
+        return fail(ctx, RF_ERR_INVALID, "%s", e.what());
+    }
+    int rc = jit_compile(ctx, p->plan.key, p->plan.source, p->mod, nullptr);
+    if (rc) return rc;
+    for (auto& k : p->plan.kernels) {
+        CUfunction f;
+        if ((rc = get_function(ctx, *p->mod, k.name, f))) return rc;
+        if (k.smem > 48 * 1024) {
+            CUresult cr = drv().FuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)k.smem);
+            if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "cuFuncSetAttribute");
+        }
+        p->fns.push_back(f);
+    }
+    // work units of the main kernel: enough resident blocks to fill the GPU once
+    int per_sm = 1;
+    for (size_t i = 0; i < p->plan.kernels.size(); i++) {
+        if (p->plan.kernels[i].role != rfg::KernelSpec::MAIN) continue;
+        CUresult cr = drv().OccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fns[i], p->plan.kernels[i].threads,
+                                                                      p->plan.kernels[i].smem);
+        if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "occupancy query");
+        if (per_sm < 1) return fail(ctx, RF_ERR_JIT, "kernel %s cannot be resident (too many resources)", p->plan.kernels[i].name.c_str());
+    }
+    p->max_units = ctx->sm_count * per_sm;
+    p->partials_bytes = (size_t)p->max_units * (p->plan.acc_bytes ? p->plan.acc_bytes : 8);
+    CUDA_TRY(ctx, cudaMalloc(&p->partials, p->partials_bytes));
+    CUDA_TRY(ctx, cudaMalloc((void**)&p->counter, 64));
+    CUDA_TRY(ctx, cudaMemset(p->counter, 0, 64));
+    CUDA_TRY(ctx, cudaMalloc((void**)&p->range, 64));
+    size_t osz = p->plan.out_size ? p->plan.out_size : 8;
+    CUDA_TRY(ctx, cudaMalloc((void**)&p->dout, (osz + 15) / 16 * 16));
+    *out = p.release();
+    return RF_OK;
+}
+
+extern "C" int rf_plan_check(const char* text, int vectorize, char* buf, size_t buf_len)
+{
+    auto put = [&](const std::string& m) {
+        if (buf && buf_len) {
+            size_t n = std::min(buf_len - 1, m.size());
+            memcpy(buf, m.data(), n);
+            buf[n] = 0;
+        }
+    };
+    if (!text) return RF_ERR_INVALID;
+    rfg::Plan plan;
+    try {
+        plan = rfg::lower(reffine::parse_text(text), vectorize != 0);
+    } catch (const rfg::LowerError& e) {
+        put(e.what());
+        return e.unsupported ? RF_ERR_UNSUPPORTED : RF_ERR_INVALID;
+    } catch (const std::exception& e) {
+        put(e.what());
+        return RF_ERR_INVALID;
+    }
+    std::string cubin, log;
+    if (!nvrtc_compile(plan.source, cubin, log)) {
+        put(log);
+        return RF_ERR_JIT;
+    }
+    put(plan.source);
+    return RF_OK;
+}
+
+extern "C" int rf_plan_free(rf_plan* p)
+{
+    if (!p) return RF_OK;
+    cudaSetDevice(p->ctx->device);
+    cudaStreamSynchronize(p->ctx->stream);
+    cudaFree(p->partials);
+    cudaFree(p->counter);
+    cudaFree(p->range);
+    cudaFree(p->dout);
+    for (auto* t : p->staging)
+        if (t) {
+            free_table_mem(t);
+            delete t;
+        }
+    rfrt::thunk_release(p);
+    delete p;
+    return RF_OK;
+}
+
+extern "C" const char* rf_plan_source(rf_plan* p) { return p ? p->plan.source.c_str() : ""; }
+
+extern "C" int rf_plan_info(rf_plan* p, rf_plan_info_t* info)
+{
+    if (!p || !info) return RF_ERR_INVALID;
+    memset(info, 0, sizeof(*info));
+    info->kind = (int)p->plan.kind;
+    info->n_inputs = p->plan.n_inputs;
+    info->output_is_table = p->plan.out_is_table;
+    info->n_groups = p->plan.groups;
+    info->output_size = (int64_t)p->plan.out_size;
+    for (int i = 0; i < p->plan.n_inputs && i < 8; i++) {
+        long long b = 0;
+        if (p->plan.input_types[i].is_vector())
+            for (int c : p->plan.cols_read[i]) b += (long long)p->plan.input_types[i].dtypes[c].size();
+        info->bytes_per_row[i] = b;
+    }
+    info->n_kernels = (int32_t)p->plan.kernels.size();
+    info->vectorize = p->plan.vectorize;
+    return RF_OK;
+}
+
+namespace rfrt {
+
+int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long long& lo, long long& hi)
+{
+    rf_ctx* ctx = p->ctx;
+    const rfg::Plan& pl = p->plan;
+    if (n_args != pl.n_inputs) return fail(ctx, RF_ERR_INVALID, "plan takes %d inputs, got %d", pl.n_inputs, n_args);
+    memset(&P, 0, sizeof(P));
+    for (int i = 0; i < n_args; i++) {
+        const auto& ty = pl.input_types[i];
+        if (ty.is_vector()) {
+            if (args[i].kind != RF_ARG_TABLE || !args[i].table)
+                return fail(ctx, RF_ERR_INVALID, "input %d must be a table", i);
+            rf_table* t = args[i].table;
+            if (t->cols.size() != ty.dtypes.size())
+                return fail(ctx, RF_ERR_INVALID, "input %d: table has %zu columns, query expects %zu", i, t->cols.size(),
+                            ty.dtypes.size());
+            RfTab& T = P.t[pl.table_slot[i]];
+            for (size_t c = 0; c < t->cols.size(); c++) {
+                auto& dc = t->cols[c];
+                if (dc.type.size() != ty.dtypes[c].size() || dc.type.is_float() != ty.dtypes[c].is_float())
+                    return fail(ctx, RF_ERR_INVALID, "input %d column %zu: type %s, query expects %s", i, c,
+                                dc.type.str().c_str(), ty.dtypes[c].str().c_str());
+                if ((ty.encodings[c] == reffine::RUNEND) != dc.runend)
+                    return fail(ctx, RF_ERR_INVALID, "input %d column %zu: encoding differs from the query's", i, c);
+                T.col[c].data = dc.data;
+                T.col[c].valid = dc.valid;
+                T.col[c].run_ends = dc.run_ends;
+                T.col[c].len = dc.nvals;
+            }
+            for (int c : pl.cols_read[i])
+                if (!t->present[c]) return fail(ctx, RF_ERR_INVALID, "input %d: column %d is not on the device", i, c);
+            if (pl.needs_index[i]) {
+                if (!t->has_index) {
+                    int rc = build_index(t, ctx->stream);
+                    if (rc) return rc;
+                }
+                T.ix.slots = t->ix_slots;
+                T.ix.cap = t->ix_cap;
+                T.ix.special = t->ix_special;
+            }
+            T.nrows = t->cols.empty() ? 0 : t->cols[0].logical;
+        } else {
+            int j = pl.scalar_slot[i];
+            if (ty.is_float()) {
+                double d = args[i].kind == RF_ARG_F64 ? args[i].f64 : (double)args[i].i64;
+                memcpy(&P.s[j], &d, 8);
+            } else {
+                P.s[j] = args[i].kind == RF_ARG_F64 ? (long long)args[i].f64 : args[i].i64;
+            }
+        }
+    }
+    for (size_t k = 0; k < pl.consts.size(); k++) {
+        if (pl.consts[k].is_float) P.k[k].f = pl.consts[k].f;
+        else P.k[k].i = pl.consts[k].i;
+    }
+    bool ok = true;
+    lo = eval_host(pl.row_lo, args, n_args, ok);
+    hi = eval_host(pl.row_hi, args, n_args, ok);
+    if (!ok) return fail(ctx, RF_ERR_INVALID, "cannot evaluate the loop bounds");
+    if (pl.drive_input >= 0) {
+        // never read past the driving table's columns (the reference would read out of bounds)
+        rf_table* t = args[pl.drive_input].table;
+        for (int c : pl.cols_read[pl.drive_input])
+            if (t->cols[c].nvals < hi) hi = t->cols[c].nvals;
+        if (lo < 0) lo = 0;
+    }
+    if (hi < lo) hi = lo;
+    P.row_lo = lo;
+    P.row_hi = hi;
+    P.tile_rows = pl.tile_rows;
+    P.range = pl.device_range ? p->range : nullptr;
+    P.partials = p->partials;
+    P.counter = p->counter;
+    P.out = p->dout;
+    P.err = ctx->dev_err;
+    return RF_OK;
+}
+
+int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams* Pout)
+{
+    rf_ctx* ctx = p->ctx;
+    RfParams P;
+    long long lo, hi;
+    int rc = fill_params(p, args, n_args, P, lo, hi);
+    if (rc) return rc;
+    const rfg::Plan& pl = p->plan;
+    long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
+    int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+    P.nunits = units;
+    for (size_t i = 0; i < pl.kernels.size(); i++) {
+        const auto& k = pl.kernels[i];
+        int grid = 1;
+        switch (k.role) {
+            case rfg::KernelSpec::RANGE: grid = 1; break;
+            case rfg::KernelSpec::STOP: grid = (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8); break;
+            case rfg::KernelSpec::MAIN: grid = units; break;
+            default: grid = units; break;
+        }
+        if ((rc = launch(ctx, p->fns[i], grid, k.threads, k.smem, s, &P))) return rc;
+    }
+    if (Pout) *Pout = P;
+    return RF_OK;
+}
+
+}  // namespace rfrt
+
+namespace rfrt {
+const rfg::Plan& plan_of(rf_plan* p) { return p->plan; }
+rf_ctx* ctx_of(rf_plan* p) { return p->ctx; }
+std::vector<rf_table*>& staging_of(rf_plan* p)
+{
+    if (p->staging.size() < (size_t)p->plan.n_inputs) p->staging.resize(p->plan.n_inputs, nullptr);
+    return p->staging;
+}
+}  // namespace rfrt
+
+extern "C" int rf_plan_launch(rf_plan* p, const rf_arg* args, int32_t n_args, void* dev_out, void* stream)
+{
+    if (!p) return RF_ERR_INVALID;
+    rf_ctx* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    if (p->plan.out_is_table) return fail(ctx, RF_ERR_INVALID, "rf_plan_launch takes value-output plans");
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    int rc = enqueue(p, args, n_args, s, nullptr);
+    if (rc) return rc;
+    if (dev_out) CUDA_TRY(ctx, cudaMemcpyAsync(dev_out, p->dout, p->plan.out_size, cudaMemcpyDeviceToDevice, s));
+    return RF_OK;
+}
+
+extern "C" int rf_plan_run(rf_plan* p, const rf_arg* args, int32_t n_args, void* out, void* stream)
+{
+    if (!p) return RF_ERR_INVALID;
+    rf_ctx* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    if (p->plan.out_is_table) return fail(ctx, RF_ERR_UNSUPPORTED, "table outputs are not available yet");
+    int rc = enqueue(p, args, n_args, s, nullptr);
+    if (rc) return rc;
+    if (out) CUDA_TRY(ctx, cudaMemcpyAsync(out, p->dout, p->plan.out_size, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return check_device_error(ctx);
+}

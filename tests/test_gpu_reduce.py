@@ -1,0 +1,101 @@
+"""GPU parity of the scan-reduce templates against the oracle (same seeded inputs).
+
+Integers (counts, integer sums) must be bit-exact; FP64 sums within RTOL_F64 (parity.py).
+Sizes are chosen so the oracle finishes in seconds and tails are ragged (not multiples of a
+tile or a warp).
+"""
+import numpy as np
+import pytest
+
+import refqueries as rq
+from oracle import loopgen
+from parity import assert_same
+from reffine_gb300 import _capi, engine, workloads as W
+from reffine_gb300.table import Table, pack_validity
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n", [0, 1, 1000, 257_123, 1_000_003])
+def test_filter_sum_parity(eng, n):
+    t = W.filter_sum_table(n, seed=5)
+    fn = W.filter_sum_query(t.get_data_type())
+    ref = loopgen.Query(fn)(t)
+    got = eng.compile(fn).run(eng.upload(t))
+    assert_same(got, ref)
+    if n > 1000:
+        assert ref[1] > 0
+
+
+def test_filter_sum_random_constants_share_module(eng):
+    t = W.filter_sum_table(300_001, seed=9)
+    dt = eng.upload(t)
+    rng = np.random.default_rng(0)
+    for _ in range(4):
+        lo = int(rng.integers(0, 2000))
+        hi = lo + int(rng.integers(1, 600))
+        dlo = round(float(rng.integers(0, 8)) / 100, 6)
+        fn = W.filter_sum_query(t.get_data_type(), lo, hi, dlo, dlo + 0.02, float(rng.integers(2, 50)))
+        assert_same(eng.compile(fn).run(dt), loopgen.Query(fn)(t))
+
+
+@pytest.mark.parametrize("vectorize", [False, True])
+def test_groupby_parity(eng, vectorize):
+    t = W.groupby_table(1_234_567, seed=7)
+    fn = W.groupby_query(t.get_data_type())
+    plan = eng.compile(fn, vectorize)
+    assert plan.kind == 2  # grouped template
+    got = plan.run(eng.upload(t))
+    ref = loopgen.Query(fn, vectorize)(t)
+    assert_same(got, ref)
+
+
+def test_join_parity(eng):
+    b, p = W.join_tables(100_003, 1_500_007, seed=11)
+    fn = W.join_query(b.get_data_type(), p.get_data_type())
+    got = eng.compile(fn).run(eng.upload(b), eng.upload(p))
+    ref = loopgen.Query(fn)(b, p)
+    assert_same(got, ref)
+    assert sum(g[1] for g in ref) > 0
+
+
+def test_validity_of_column_one_gates_rows(eng):
+    # loopgen.cpp:238: a SubVector reduce skips rows whose column-1 value is null
+    t = W.filter_sum_table(100_000, seed=3)
+    mask = np.random.default_rng(1).random(len(t)) < 0.7
+    t.columns[1].valid = pack_validity(mask)
+    fn = W.filter_sum_query(t.get_data_type())
+    assert_same(eng.compile(fn).run(eng.upload(t)), loopgen.Query(fn)(t))
+
+
+@pytest.mark.parametrize("vectorize", [False, True])
+def test_reference_reduce_goldens_on_gpu(eng, vectorize):
+    st2 = rq.students_table(2)
+    assert eng.compile(rq.sum_col1_op(st2), vectorize).run(eng.upload(st2)) == 131977
+    st = rq.students_table()
+    assert eng.compile(rq.vector_op(st), vectorize).run(eng.upload(st)) == 696
+
+
+def test_thunk_has_reference_call_shape(eng):
+    # compile_op returns a function called as fn(&out, ArrowTable*): host tables in, result out
+    t = W.filter_sum_table(200_003, seed=13)
+    fn = W.filter_sum_query(t.get_data_type())
+    q = engine.compile_op(fn, engine=eng)
+    assert_same(q(t), loopgen.Query(fn)(t))
+    st = rq.students_table()
+    assert engine.compile_op(rq.vector_op(st), engine=eng)(st) == 696
+
+
+def test_missing_lower_bound_reports_error(eng):
+    # ReduceOpTest's space starts at Locate(max(lb, col0[0])); a key absent from the iterator
+    # column makes the reference read row -1.  Here the run fails with RF_ERR_DEVICE.
+    st = rq.students_table()
+    ids = st.columns[0].data.copy()
+    ids[9] = 10_000_000  # no id 10 any more
+    st.columns[0].data = ids
+    with pytest.raises(_capi.RfError) as e:
+        eng.compile(rq.vector_op(st)).run(eng.upload(st))
+    assert e.value.status == _capi.RF_ERR_DEVICE
+    # the context stays usable
+    st = rq.students_table()
+    assert eng.compile(rq.vector_op(st)).run(eng.upload(st)) == 696
