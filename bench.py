@@ -136,25 +136,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
-def build_workload(config: int, rank: int, world: int):
+def build_workload(config: int, rank: int, world: int, rows: int = 0):
     """Returns (name, tables list, query Func, rows, config dict).  Each rank gets its own
     partition (a different seed), so per-GPU work is fixed as N grows."""
     from reffine_gb300 import workloads as W
     seed_off = 1000 * rank
     if config == 0:
-        n = 6_000_000
+        n = rows or 6_000_000
         t = W.filter_sum_table(n, seed=0 + seed_off)
         return ("filter_sum_6M", [t], W.filter_sum_query(t.get_data_type()), n,
                 {"rows": n, "query": "SUM(price*discount), COUNT over day in [730,1095), discount in [0.05,0.07], "
                                      "quantity < 24"})
     if config == 1:
-        n = 60_000_000
+        n = rows or 60_000_000
         t = W.groupby_table(n, seed=1 + seed_off)
         return ("groupby_6groups_60M", [t], W.groupby_query(t.get_data_type()), n,
                 {"rows": n, "groups": 6, "query": "per (flag_a, flag_b): SUM qty/price/disc_price/charge, AVG "
                                                   "qty/price/disc, COUNT over day <= 2450"})
     if config == 3:
-        nb, npr = 10_000_000, 200_000_000
+        nb, npr = 10_000_000, rows or 200_000_000
         b, p = W.join_tables(nb, npr, seed=3 + seed_off)
         return ("join_10M_x_200M", [b, p], W.join_query(b.get_data_type(), p.get_data_type()), npr,
                 {"rows": npr, "build_rows": nb, "query": "SUM(amount), COUNT per build attr < 5, probe day in [0,365)"})
@@ -189,7 +189,7 @@ def cpu_baseline(fn, tables, nbytes, budget_s=20.0):
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    name, tables, fn, rows, cfg = build_workload(args.config, 0, 1)
+    name, tables, fn, rows, cfg = build_workload(args.config, 0, 1, args.rows)
     from reffine_gb300 import engine
     # algorithmic bytes come from the lowering's column analysis (no GPU needed for it)
     from oracle import loopgen
@@ -239,6 +239,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rows", type=int, default=0, help="override the row count (profiling a smaller case)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -247,7 +248,7 @@ def main():
     from reffine_gb300 import cudart, engine
     dist = Dist(world)
     eng = engine.Engine(local)
-    name, tables, fn, rows, cfg = build_workload(args.config, rank, world)
+    name, tables, fn, rows, cfg = build_workload(args.config, rank, world, args.rows)
     dts = [eng.upload(t) for t in tables]
     plan = eng.compile(fn)
     nbytes = referenced_bytes(plan, tables)
@@ -295,8 +296,12 @@ def main():
 
     # end to end through the reference-shaped call: host tables in pinned memory
     e2e = None
+    if args.e2e_steps <= 0:
+        args.e2e_steps = 0
     h2d = sum(int(plan.info.bytes_per_row[i]) * len(t) for i, t in enumerate(tables))
     try:
+        if not args.e2e_steps:
+            raise RuntimeError("e2e skipped (--e2e-steps 0)")
         from reffine_gb300.table import Column, Table
         pinned = []
         ptables = []

@@ -450,8 +450,9 @@ class Gen:
     def ctype(self, t: ir.DataType) -> str:
         if t.is_struct():
             if t not in self.typedefs:
-                nm = "_%d_t" % len(self.typedefs)
+                # field types first: nested structs get their typedefs (and names) before this one
                 fields = " ".join("%s _%d;" % (self.ctype(d), i) for i, d in enumerate(t.dtypes))
+                nm = "_%d_t" % len(self.typedefs)
                 self.typedefs[t] = nm
                 self.header.append("typedef struct { %s } %s;" % (fields, nm))
             return self.typedefs[t]

@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -275,8 +276,29 @@ public:
             if (reds.size() != 1) throw LowerError("the GPU backend lowers Funcs with exactly one Reduce");
             lower_reduce(*reds[0]);
         }
+        derive_cols_read();
         plan_.key = hexkey(plan_.source);
         return plan_;
+    }
+
+    // the columns a plan reads are exactly those its generated source references
+    // (P.t[slot].col[c]); table uploads and byte accounting use this set
+    void derive_cols_read()
+    {
+        const std::string& s = plan_.source;
+        const std::string pat = "P.t[";
+        for (size_t pos = s.find(pat); pos != std::string::npos; pos = s.find(pat, pos + 1)) {
+            size_t a = pos + pat.size();
+            size_t b = s.find("].col[", a);
+            if (b == std::string::npos || b - a > 2) continue;
+            size_t c0 = b + 6, c1 = s.find(']', c0);
+            if (c1 == std::string::npos || c1 - c0 > 3) continue;
+            int slot = std::atoi(s.substr(a, b - a).c_str());
+            int col = std::atoi(s.substr(c0, c1 - c0).c_str());
+            for (size_t i = 0; i < plan_.table_slot.size(); i++)
+                if (plan_.table_slot[i] == slot) note_col((int)i, (size_t)col);
+        }
+        for (auto& v : plan_.cols_read) std::sort(v.begin(), v.end());
     }
 
 private:
