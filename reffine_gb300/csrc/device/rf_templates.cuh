@@ -165,3 +165,198 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
     }
 #endif  // RF_GROUP_REDUCE
 
+
+// ---------------------------------------------------------------------------------------
+// Template 3: Op materialisation (LoopGen::visit(Op), loopgen.cpp:113-204, and
+// finalize_vector, vinstr.h:113-135).
+//   The fragment defines rf_cond(P, r) (the iteration condition of element r) and
+//   rf_emit(P, r, o) (computes the element's iterators and outputs, writes them at output row o).
+//   Output columns: ((void**)P.aux0)[c]; validity words: ((unsigned**)P.aux1)[c];
+//   per-tile counts / offsets: (long long*)P.aux2; results (long long*)P.aux3:
+//   [0] = rows written, [1] = null count.
+//   Compaction (vectorize off) keeps passing elements in loop order: count per tile, one
+//   exclusive scan over tiles, then a scatter that ranks elements inside each tile with warp
+//   ballots.  Vectorised (on): every visited element is written; its condition becomes the
+//   validity bit.
+// ---------------------------------------------------------------------------------------
+#ifdef RF_MATERIALIZE
+RF_DEV void rf_mat_bounds(const RfParams& P, long long& lo, long long& hi)
+{
+    lo = P.row_lo;
+    hi = P.row_hi;
+    if (P.range) {
+        long long b = P.range[0], e = P.range[1];
+        lo = b > lo ? b : lo;
+        hi = e < hi ? e : hi;
+    }
+}
+
+RF_DEV long long rf_mat_ntiles(const RfParams& P)
+{
+    return (P.row_hi - P.row_lo + P.tile_rows - 1) / P.tile_rows;
+}
+
+template <int T>
+RF_DEV int rf_block_sum_int(int v, int* sh)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = __reduce_add_sync(0xffffffffu, v);
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    int t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < T / 32; w++) t += sh[w];
+    __syncthreads();
+    return t;
+}
+
+template <int T>
+RF_DEV void rf_mat_count(const RfParams& P)
+{
+    __shared__ int sh[T / 32];
+    long long lo, hi;
+    rf_mat_bounds(P, lo, hi);
+    long long* cnt = (long long*)P.aux2;
+    const long long nt = rf_mat_ntiles(P);
+    for (long long tile = blockIdx.x; tile < nt; tile += gridDim.x) {
+        long long r0 = P.row_lo + tile * P.tile_rows, r1 = r0 + P.tile_rows;
+        if (r1 > hi) r1 = hi;
+        if (r0 < lo) r0 = lo;
+        int c = 0;
+        for (long long r = r0 + threadIdx.x; r < r1; r += T) c += rf_cond(P, r) ? 1 : 0;
+        int t = rf_block_sum_int<T>(c, sh);
+        if (threadIdx.x == 0) cnt[tile] = t;
+    }
+}
+
+// exclusive scan of the tile counts in place (one block); total -> aux3[0]
+RF_DEV void rf_mat_scan(const RfParams& P)
+{
+    __shared__ long long wsum[32];
+    __shared__ long long carry;
+    long long* cnt = (long long*)P.aux2;
+    const long long nt = rf_mat_ntiles(P);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (long long base = 0; base < nt; base += blockDim.x) {
+        long long i = base + threadIdx.x;
+        long long v = i < nt ? cnt[i] : 0;
+        long long x = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                long long y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= off) w += y;
+            }
+            if (lane < nw) wsum[lane] = w;
+        }
+        __syncthreads();
+        long long excl = carry + (warp ? wsum[warp - 1] : 0) + x - v;
+        if (i < nt) cnt[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += wsum[nw - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) ((long long*)P.aux3)[0] = carry;
+}
+
+template <int T>
+RF_DEV void rf_mat_scatter(const RfParams& P)
+{
+    __shared__ int wcnt[T / 32];
+    __shared__ int woff[T / 32 + 1];
+    long long lo, hi;
+    rf_mat_bounds(P, lo, hi);
+    const long long* off = (const long long*)P.aux2;
+    const long long nt = rf_mat_ntiles(P);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (long long tile = blockIdx.x; tile < nt; tile += gridDim.x) {
+        long long r0 = P.row_lo + tile * P.tile_rows, r1 = r0 + P.tile_rows;
+        if (r1 > hi) r1 = hi;
+        if (r0 < lo) r0 = lo;
+        long long base = off[tile];
+        for (long long c0 = r0; c0 < r1; c0 += T) {
+            long long r = c0 + threadIdx.x;
+            bool c = r < r1 && rf_cond(P, r);
+            unsigned m = __ballot_sync(0xffffffffu, c);
+            if (lane == 0) wcnt[warp] = __popc(m);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int s = 0;
+                for (int w = 0; w < T / 32; w++) {
+                    woff[w] = s;
+                    s += wcnt[w];
+                }
+                woff[T / 32] = s;
+            }
+            __syncthreads();
+            if (c) rf_emit(P, r, base + woff[warp] + __popc(m & ((1u << lane) - 1u)));
+            base += woff[T / 32];
+            __syncthreads();
+        }
+    }
+}
+
+template <int T>
+RF_DEV void rf_mat_write_all(const RfParams& P, int ncols)
+{
+    long long lo, hi;
+    rf_mat_bounds(P, lo, hi);
+    const long long nt = rf_mat_ntiles(P);
+    const int lane = threadIdx.x & 31;
+    long long nulls = 0;
+    for (long long tile = blockIdx.x; tile < nt; tile += gridDim.x) {
+        long long r0 = P.row_lo + tile * P.tile_rows, r1 = r0 + P.tile_rows;
+        if (r1 > hi) r1 = hi;
+        if (r0 < lo) r0 = lo;
+        for (long long c0 = r0; c0 < r1; c0 += T) {
+            long long r = c0 + threadIdx.x;
+            bool in = r < r1;
+            bool c = in && rf_cond(P, r);
+            if (in) rf_emit(P, r, r - lo);
+            unsigned m = __ballot_sync(0xffffffffu, c);
+            unsigned act = __ballot_sync(0xffffffffu, in);
+            nulls += (lane == 0) ? __popc(act & ~m) : 0;
+            // lanes of a warp hold consecutive elements: their bits land in at most two words
+            long long o0 = __shfl_sync(0xffffffffu, r - lo, 0);
+            if (lane == 0 && act) {
+                long long w = o0 >> 5;
+                int sft = (int)(o0 & 31);
+                for (int col = 0; col < ncols; col++) {
+                    unsigned* bm = ((unsigned**)P.aux1)[col];
+                    atomicOr(bm + w, m << sft);
+                    if (sft && (m >> (32 - sft))) atomicOr(bm + w + 1, m >> (32 - sft));
+                }
+            }
+        }
+    }
+    if (lane == 0 && nulls) atomicAdd((unsigned long long*)P.aux3 + 1, (unsigned long long)nulls);
+}
+
+#define RF_MATERIALIZE_KERNELS(T, NCOLS)                                                                  \
+    extern "C" __global__ void __launch_bounds__(T) rf_count(const __grid_constant__ RfParams P)         \
+    {                                                                                                    \
+        rf_mat_count<T>(P);                                                                              \
+    }                                                                                                    \
+    extern "C" __global__ void __launch_bounds__(1024) rf_scan(const __grid_constant__ RfParams P)      \
+    {                                                                                                    \
+        rf_mat_scan(P);                                                                                  \
+    }                                                                                                    \
+    extern "C" __global__ void __launch_bounds__(T) rf_scatter(const __grid_constant__ RfParams P)       \
+    {                                                                                                    \
+        rf_mat_scatter<T>(P);                                                                            \
+    }                                                                                                    \
+    extern "C" __global__ void __launch_bounds__(T) rf_write_all(const __grid_constant__ RfParams P)     \
+    {                                                                                                    \
+        rf_mat_write_all<T>(P, NCOLS);                                                                   \
+    }
+#endif  // RF_MATERIALIZE

@@ -1616,10 +1616,119 @@ private:
     }
 
     // ---------------------------------------------------------------- Op lowering (tables)
+    // binds the Op's iterator for element r of its iteration space; returns the element's
+    // iteration condition (VecSpace: r < len && valid(col0, r); bounds; filter symbols)
+    std::string bind_op_row(Emitter& E, const Op& op, const Drive& d, std::ostringstream& body)
+    {
+        const Space& sp = d.sp;
+        std::string T = ctype(sp.iter->type);
+        std::string sl = std::to_string(d.slot);
+        std::string it_c, cond;
+        if (sp.has_vec) {
+            note_col(d.input, 0);
+            it_c = "rf_ld<" + T + ">(P.t[" + sl + "].col[0].data, r)";
+            cond = "rf_valid(P.t[" + sl + "].col[0].valid, r)";
+            E.vec_iter_idx[{sp.vec_node.get(), sp.iter.get()}] = "r";
+        } else {
+            it_c = "((" + T + ")r)";
+            cond = "true";
+        }
+        body << "    const " << T << " it = " << it_c << ";\n";
+        E.bind(op.iters[0], E.scalar("it", sp.iter->type));
+        if (!sp.lbs.empty()) cond += " && (it >= (" + T + ")P.range[2])";
+        if (!sp.ubs.empty()) cond += " && (it <= (" + T + ")P.range[3])";
+        for (auto& f : sp.filters) cond += " && (" + E.ev(f).c + ")";
+        return cond;
+    }
+
+    void drive_rows(Drive& d)
+    {
+        if (d.sp.has_vec) {
+            d.input = d.sp.vec_input;
+            d.slot = plan_.table_slot[d.input];
+            plan_.drive_input = d.input;
+            HostExpr lo;
+            lo.kind = HostExpr::CONST;
+            lo.value = 0;
+            HostExpr hi;
+            hi.kind = HostExpr::LEN;
+            hi.input = d.input;
+            hi.col = 0;
+            plan_.row_lo = lo;
+            plan_.row_hi = hi;
+        } else {
+            plan_.row_lo = minmax_host(d.sp.lbs, true);
+            HostExpr hi = minmax_host(d.sp.ubs, false);
+            HostExpr one;
+            one.kind = HostExpr::CONST;
+            one.value = 1;
+            HostExpr h2;
+            h2.kind = HostExpr::ADD;
+            h2.args = {hi, one};
+            plan_.row_hi = h2;
+        }
+    }
+
     void lower_op(const Expr& opx)
     {
-        (void)opx;
-        throw LowerError("Op outputs are lowered by the materialisation templates (not yet available)");
+        const Op& op = *as<Op>(opx);
+        plan_.out_is_table = true;
+        plan_.out_dim = (int)op.iters.size();
+        for (auto& i : op.iters) plan_.out_cols.push_back(i->type);
+        for (auto& o : op.outputs) {
+            if (!o->type.is_primitive()) throw LowerError("data type not supported " + o->type.str(), false);
+            plan_.out_cols.push_back(o->type);
+        }
+        if ((int)plan_.out_cols.size() > RF_MAX_COLS_) throw LowerError("too many output columns");
+        Drive d;
+        d.sp = op_space(op);
+        drive_rows(d);
+        plan_.kind = PlanKind::MATERIALIZE;
+        const int T = plan_.threads;
+        std::ostringstream src;
+        src << "// generated by the reffine_gb300 lowering pass: " << fn_->name << " (Op materialisation)\n";
+        src << "#include \"rf_device.cuh\"\n\n";
+        emit_range_kernels(src, d);
+        {
+            Emitter E(*this);
+            bind_inputs(E);
+            std::ostringstream body;
+            std::string cond = bind_op_row(E, op, d, body);
+            src << "RF_DEV bool rf_cond(const RfParams& P, long long r)\n{\n" << body.str();
+            for (auto& dcl : E.decls) src << "    " << dcl << "\n";
+            src << "    return " << cond << ";\n}\n\n";
+        }
+        {
+            Emitter E(*this);
+            bind_inputs(E);
+            std::ostringstream body;
+            bind_op_row(E, op, d, body);
+            std::ostringstream w;
+            size_t c = 0;
+            for (auto& i : op.iters) {
+                w << "    ((" << ctype(i->type) << "*)((void* const*)P.aux0)[" << c << "])[o] = (" << ctype(i->type)
+                  << ")(" << E.ev(i).c << ");\n";
+                c++;
+            }
+            for (auto& o : op.outputs) {
+                w << "    ((" << ctype(o->type) << "*)((void* const*)P.aux0)[" << c << "])[o] = (" << ctype(o->type)
+                  << ")(" << E.ev(o).c << ");\n";
+                c++;
+            }
+            src << "RF_DEV void rf_emit(const RfParams& P, long long r, long long o)\n{\n" << body.str();
+            for (auto& dcl : E.decls) src << "    " << dcl << "\n";
+            src << w.str() << "}\n\n";
+        }
+        src << "#define RF_MATERIALIZE 1\n#include \"rf_templates.cuh\"\n";
+        src << "RF_MATERIALIZE_KERNELS(" << T << ", " << plan_.out_cols.size() << ")\n";
+        if (vectorize_) {
+            plan_.kernels.push_back({"rf_write_all", T, 0, KernelSpec::FINAL});
+        } else {
+            plan_.kernels.push_back({"rf_count", T, 0, KernelSpec::COUNT});
+            plan_.kernels.push_back({"rf_scan", 1024, 0, KernelSpec::SCAN});
+            plan_.kernels.push_back({"rf_scatter", T, 0, KernelSpec::SCATTER});
+        }
+        plan_.source = src.str();
     }
 
     std::shared_ptr<Func> fn_;

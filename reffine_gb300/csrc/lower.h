@@ -53,7 +53,7 @@ struct KernelSpec {
     std::string name;
     int threads = 256;
     size_t smem = 0;
-    enum Role { MAIN, RANGE, STOP, COUNT, SCATTER, INIT, FINAL } role = MAIN;
+    enum Role { MAIN, RANGE, STOP, COUNT, SCAN, SCATTER, INIT, FINAL } role = MAIN;
 };
 
 struct Plan {

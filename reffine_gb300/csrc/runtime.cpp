@@ -145,7 +145,11 @@ struct rf_plan {
     unsigned char* dout = nullptr;
     int max_units = 0;
     int thunk_slot = -1;
-    std::vector<std::unique_ptr<rf_table>> thunk_outputs;
+    // table outputs
+    void** d_ptrs = nullptr;          // device array: output column pointers, then bitmap pointers
+    long long* d_tiles = nullptr;     // per-tile counts / offsets
+    size_t tiles_cap = 0;
+    long long* d_res = nullptr;       // [rows written, null count]
 };
 
 // ------------------------------------------------------------------------------------------
@@ -843,6 +847,10 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
     CUDA_TRY(ctx, cudaMalloc((void**)&p->range, 64));
     size_t osz = p->plan.out_size ? p->plan.out_size : 8;
     CUDA_TRY(ctx, cudaMalloc((void**)&p->dout, (osz + 15) / 16 * 16));
+    if (p->plan.out_is_table) {
+        CUDA_TRY(ctx, cudaMalloc((void**)&p->d_ptrs, sizeof(void*) * 2 * RF_MAX_COLS));
+        CUDA_TRY(ctx, cudaMalloc((void**)&p->d_res, 64));
+    }
     *out = p.release();
     return RF_OK;
 }
@@ -885,6 +893,9 @@ extern "C" int rf_plan_free(rf_plan* p)
     cudaFree(p->counter);
     cudaFree(p->range);
     cudaFree(p->dout);
+    cudaFree(p->d_ptrs);
+    cudaFree(p->d_tiles);
+    cudaFree(p->d_res);
     for (auto* t : p->staging)
         if (t) {
             free_table_mem(t);
@@ -1012,6 +1023,7 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
         int grid = 1;
         switch (k.role) {
             case rfg::KernelSpec::RANGE: grid = 1; break;
+            case rfg::KernelSpec::SCAN: grid = 1; break;
             case rfg::KernelSpec::STOP: grid = (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8); break;
             case rfg::KernelSpec::MAIN: grid = units; break;
             default: grid = units; break;
@@ -1047,13 +1059,123 @@ extern "C" int rf_plan_launch(rf_plan* p, const rf_arg* args, int32_t n_args, vo
     return RF_OK;
 }
 
+namespace {
+
+// Runs an Op plan: allocates the output table (capacity = the loop's row range, so no 1e8-row
+// preallocation as in loopgen.cpp:115), launches the materialisation kernels and sizes the table
+// from the device counters (finalize_vector, vinstr.h:113-135).
+int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaStream_t s)
+{
+    rf_ctx* ctx = p->ctx;
+    const rfg::Plan& pl = p->plan;
+    RfParams P;
+    long long lo, hi;
+    int rc = fill_params(p, args, n_args, P, lo, hi);
+    if (rc) return rc;
+    long long cap = hi - lo;
+    size_t nc = pl.out_cols.size();
+    auto t = std::make_unique<rf_table>();
+    t->ctx = ctx;
+    t->dim = pl.out_dim;
+    t->name = "out";
+    t->cols.resize(nc);
+    t->present.assign(nc, 1);
+    std::vector<void*> hptrs(2 * RF_MAX_COLS, nullptr);
+    for (size_t c = 0; c < nc; c++) {
+        DevCol& dc = t->cols[c];
+        dc.type = pl.out_cols[c];
+        dc.name = (c < (size_t)pl.out_dim ? "it" : "out") + std::to_string(c < (size_t)pl.out_dim ? c : c - pl.out_dim);
+        size_t bytes = (size_t)std::max<long long>(cap, 1) * dc.type.size();
+        if (cudaMalloc(&dc.data_buf, bytes + 16) != cudaSuccess) {
+            free_table_mem(t.get());
+            return fail(ctx, RF_ERR_OOM, "output column allocation (%zu bytes) failed", bytes);
+        }
+        dc.data_cap = bytes;
+        dc.data = dc.data_buf;
+        hptrs[c] = dc.data_buf;
+        if (pl.vectorize) {
+            size_t vb = (size_t)((std::max<long long>(cap, 1) + 31) / 32) * 4;
+            if (cudaMalloc(&dc.valid_buf, vb + 16) != cudaSuccess) {
+                free_table_mem(t.get());
+                return fail(ctx, RF_ERR_OOM, "output bitmap allocation failed");
+            }
+            dc.valid_cap = vb;
+            CUDA_TRY(ctx, cudaMemsetAsync(dc.valid_buf, 0, vb + 16, s));
+            hptrs[RF_MAX_COLS + c] = dc.valid_buf;
+        }
+    }
+    long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
+    if ((size_t)std::max<long long>(ntiles, 1) > p->tiles_cap) {
+        cudaStreamSynchronize(s);
+        cudaFree(p->d_tiles);
+        p->tiles_cap = (size_t)std::max<long long>(ntiles, 1024);
+        if (cudaMalloc((void**)&p->d_tiles, p->tiles_cap * 8) != cudaSuccess) {
+            p->tiles_cap = 0;
+            free_table_mem(t.get());
+            return fail(ctx, RF_ERR_OOM, "tile buffer allocation failed");
+        }
+    }
+    CUDA_TRY(ctx, cudaMemcpyAsync(p->d_ptrs, hptrs.data(), sizeof(void*) * hptrs.size(), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(ctx, cudaMemsetAsync(p->d_res, 0, 64, s));
+    P.aux0 = p->d_ptrs;
+    P.aux1 = p->d_ptrs + RF_MAX_COLS;
+    P.aux2 = p->d_tiles;
+    P.aux3 = p->d_res;
+    int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+    P.nunits = units;
+    for (size_t i = 0; i < pl.kernels.size(); i++) {
+        const auto& k = pl.kernels[i];
+        int grid = units;
+        if (k.role == rfg::KernelSpec::RANGE || k.role == rfg::KernelSpec::SCAN) grid = 1;
+        if (k.role == rfg::KernelSpec::STOP)
+            grid = (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8);
+        if ((rc = launch(ctx, p->fns[i], grid, k.threads, k.smem, s, &P))) {
+            free_table_mem(t.get());
+            return rc;
+        }
+    }
+    long long res[2] = {0, 0}, rng[2] = {lo, hi};
+    CUDA_TRY(ctx, cudaMemcpyAsync(res, p->d_res, 16, cudaMemcpyDeviceToHost, s));
+    if (pl.device_range) CUDA_TRY(ctx, cudaMemcpyAsync(rng, p->range, 16, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    rc = check_device_error(ctx);
+    if (rc) {
+        free_table_mem(t.get());
+        return rc;
+    }
+    long long rows = res[0];
+    if (pl.vectorize) {
+        long long a = std::max(lo, rng[0]), b = std::min(hi, rng[1]);
+        rows = b > a ? b - a : 0;
+    }
+    if (rows > cap) {
+        free_table_mem(t.get());
+        return fail(ctx, RF_ERR_DEVICE, "materialisation wrote %lld rows into %lld", rows, cap);
+    }
+    t->null_count = pl.vectorize ? res[1] : 0;
+    for (auto& dc : t->cols) {
+        dc.nvals = rows;
+        dc.logical = rows;
+        // finalize_vector: no bitmap when nothing is null
+        dc.valid = (pl.vectorize && t->null_count > 0) ? (unsigned short*)dc.valid_buf : nullptr;
+    }
+    *out = t.release();
+    return RF_OK;
+}
+
+}  // namespace
+
 extern "C" int rf_plan_run(rf_plan* p, const rf_arg* args, int32_t n_args, void* out, void* stream)
 {
     if (!p) return RF_ERR_INVALID;
     rf_ctx* ctx = p->ctx;
     cudaSetDevice(ctx->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-    if (p->plan.out_is_table) return fail(ctx, RF_ERR_UNSUPPORTED, "table outputs are not available yet");
+    if (p->plan.out_is_table) {
+        if (!out) return fail(ctx, RF_ERR_INVALID, "table output needs an rf_table** out");
+        *(rf_table**)out = nullptr;
+        return run_table(p, args, n_args, (rf_table**)out, s);
+    }
     int rc = enqueue(p, args, n_args, s, nullptr);
     if (rc) return rc;
     if (out) CUDA_TRY(ctx, cudaMemcpyAsync(out, p->dout, p->plan.out_size, cudaMemcpyDeviceToHost, s));

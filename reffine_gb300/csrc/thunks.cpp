@@ -16,6 +16,8 @@
 
 #include <array>
 #include <cstdio>
+#include <map>
+#include <memory>
 #include <cstring>
 #include <mutex>
 #include <utility>
@@ -31,6 +33,20 @@ namespace {
 constexpr int kThunks = 512;
 rf_plan* g_plans[kThunks];
 std::mutex g_mu;
+
+// a host table handed back through output_addr; its Arrow structs own their buffers
+struct HostTable : ArrowTable {
+    ArrowSchema s{};
+    ArrowArray a{};
+    explicit HostTable(int64_t dim) : ArrowTable(dim) {}
+    ~HostTable() override
+    {
+        if (a.release) a.release(&a);
+        if (s.release) s.release(&s);
+    }
+};
+// like Reffine's memman (src/engine/memory.cpp:11-16) the outputs stay alive with their plan
+std::map<rf_plan*, std::vector<std::unique_ptr<HostTable>>> g_outputs;
 
 void thunk_call(int slot, void* const* a, const double* d);
 
@@ -135,7 +151,30 @@ void thunk_call(int slot, void* const* a, const double* d)
             ar.i64 = v;
         }
     }
-    if (rc == RF_OK) rc = rf_plan_run(p, args.data(), (int32_t)args.size(), output_addr, nullptr);
+    if (rc == RF_OK) {
+        if (pl.out_is_table) {
+            // make_vector + finalize_vector hand back an ArrowTable* (loopgen.cpp:118-135, 196-199);
+            // here the device result is exported to host Arrow memory owned by the plan
+            rf_table* dt = nullptr;
+            rc = rf_plan_run(p, args.data(), (int32_t)args.size(), &dt, nullptr);
+            if (rc == RF_OK) {
+                auto* h = new HostTable(pl.out_dim);
+                rc = rf_table_export(dt, &h->s, &h->a);
+                rf_table_free(dt);
+                if (rc == RF_OK) {
+                    h->schema = &h->s;
+                    h->array = &h->a;
+                    *(ArrowTable**)output_addr = h;
+                    std::lock_guard<std::mutex> g(g_mu);
+                    g_outputs[p].emplace_back(h);
+                } else {
+                    delete h;
+                }
+            }
+        } else {
+            rc = rf_plan_run(p, args.data(), (int32_t)args.size(), output_addr, nullptr);
+        }
+    }
     if (rc != RF_OK) fprintf(stderr, "reffine_gb300: query failed (%d): %s\n", rc, rf_last_error(ctx));
 }
 
@@ -147,6 +186,7 @@ void thunk_release(rf_plan* p)
     std::lock_guard<std::mutex> g(g_mu);
     for (int i = 0; i < kThunks; i++)
         if (g_plans[i] == p) g_plans[i] = nullptr;
+    g_outputs.erase(p);
 }
 }  // namespace rfrt
 
