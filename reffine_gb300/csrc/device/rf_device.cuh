@@ -118,6 +118,26 @@ RF_DEV T rf_min(T a, T b)
 }
 
 // ---------------------------------------------------------------------------------------
+// binary64 comparisons on the integer pipe.
+// IEEE 754 orders finite values and infinities of one sign by their bit patterns read as
+// unsigned integers (sign-magnitude encoding), so key(x) = bits for x >= +0 and
+// -(bits without sign) for negative x is monotonic, and maps -0 and +0 to the same key.  A
+// comparison involving a NaN is false (== false, != true), as in IEEE and in the reference's
+// C++.  GB300 executes FP64 comparisons on its narrow FP64 pipe; these run on the integer ALUs.
+// ---------------------------------------------------------------------------------------
+RF_DEV bool rf_dnan(double x) { return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+RF_DEV long long rf_dkey(double x)
+{
+    long long b = __double_as_longlong(x);
+    return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
+RF_DEV bool rf_dlt(double a, double b) { return !rf_dnan(a) && !rf_dnan(b) && rf_dkey(a) < rf_dkey(b); }
+RF_DEV bool rf_dle(double a, double b) { return !rf_dnan(a) && !rf_dnan(b) && rf_dkey(a) <= rf_dkey(b); }
+RF_DEV bool rf_dgt(double a, double b) { return !rf_dnan(a) && !rf_dnan(b) && rf_dkey(a) > rf_dkey(b); }
+RF_DEV bool rf_dge(double a, double b) { return !rf_dnan(a) && !rf_dnan(b) && rf_dkey(a) >= rf_dkey(b); }
+RF_DEV bool rf_deq(double a, double b) { return !rf_dnan(a) && !rf_dnan(b) && rf_dkey(a) == rf_dkey(b); }
+
+// ---------------------------------------------------------------------------------------
 // hash index probe
 // ---------------------------------------------------------------------------------------
 // 64-bit finaliser of MurmurHash3 (Austin Appleby, public domain): a bijective mixer, so

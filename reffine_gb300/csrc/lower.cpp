@@ -590,11 +590,15 @@ private:
                 case MathOp::MOD: return scalar("(" + a(0) + " % " + a(1) + ")", n.type);
                 case MathOp::MAX: return scalar("rf_max<" + T + ">(" + a(0) + ", " + a(1) + ")", n.type);
                 case MathOp::MIN: return scalar("rf_min<" + T + ">(" + a(0) + ", " + a(1) + ")", n.type);
-                case MathOp::LT: return scalar("(" + a(0) + " < " + a(1) + ")", n.type);
-                case MathOp::LTE: return scalar("(" + a(0) + " <= " + a(1) + ")", n.type);
-                case MathOp::GT: return scalar("(" + a(0) + " > " + a(1) + ")", n.type);
-                case MathOp::GTE: return scalar("(" + a(0) + " >= " + a(1) + ")", n.type);
-                case MathOp::EQ: return scalar("(" + a(0) + " == " + a(1) + ")", n.type);
+                case MathOp::LT: case MathOp::LTE: case MathOp::GT: case MathOp::GTE: case MathOp::EQ: {
+                    static const char* sym[] = {"<", "<=", ">", ">=", "=="};
+                    static const char* dfn[] = {"rf_dlt", "rf_dle", "rf_dgt", "rf_dge", "rf_deq"};
+                    int k = n.op == MathOp::LT ? 0 : n.op == MathOp::LTE ? 1 : n.op == MathOp::GT ? 2 : n.op == MathOp::GTE ? 3 : 4;
+                    // binary64 comparisons go to the integer pipe (exact IEEE semantics, rf_device.cuh)
+                    if (n.args[0]->type.btype == FLOAT64)
+                        return scalar(std::string(dfn[k]) + "(" + a(0) + ", " + a(1) + ")", n.type);
+                    return scalar("(" + a(0) + " " + sym[k] + " " + a(1) + ")", n.type);
+                }
                 case MathOp::NOT: return scalar("(!" + a(0) + ")", n.type);
                 case MathOp::AND: return scalar("(" + a(0) + " && " + a(1) + ")", n.type);
                 case MathOp::OR: return scalar("(" + a(0) + " || " + a(1) + ")", n.type);
@@ -1342,6 +1346,33 @@ private:
         return r;
     }
 
+    // Loads of the driving row (rf_ld<T>(P.t[s].col[c].data, r)) that a condition reads are
+    // issued together at the top of the row function instead of one after another inside the
+    // short-circuit chain; `code` pieces are rewritten to use the hoisted locals.
+    static std::string hoist_row_loads(const std::string& cond, std::vector<std::string*> code)
+    {
+        std::ostringstream decl;
+        std::map<std::string, std::string> seen;
+        const std::string pat = "rf_ld<";
+        for (size_t pos = cond.find(pat); pos != std::string::npos; pos = cond.find(pat, pos + 1)) {
+            size_t e = cond.find(", r)", pos);
+            if (e == std::string::npos) continue;
+            std::string call = cond.substr(pos, e + 4 - pos);
+            if (call.find("P.t[") == std::string::npos || call.find('(', pat.size()) == std::string::npos) continue;
+            if (seen.count(call)) continue;
+            std::string ty = call.substr(pat.size(), call.find('>') - pat.size());
+            std::string nm = "ld" + std::to_string(seen.size());
+            seen[call] = nm;
+            decl << "    const " << ty << " " << nm << " = " << call << ";\n";
+        }
+        for (auto* c : code)
+            for (auto& kv : seen) {
+                size_t p;
+                while ((p = c->find(kv.first)) != std::string::npos) c->replace(p, kv.first.size(), kv.second);
+            }
+        return decl.str();
+    }
+
     // cost-ordered conjunction: cheap column predicates first, hash probes last
     Expr order_conjuncts(const Expr& c)
     {
@@ -1420,11 +1451,13 @@ private:
         std::string rowcond = bind_row(E, red, d, body);
         // leaves sharing a condition (structurally) are updated under one test of it
         std::ostringstream upd;
+        std::string allconds;
         std::vector<char> done(act.size(), 0);
         for (size_t k = 0; k < act.size(); k++) {
             if (done[k]) continue;
             auto& lf = leaves[act[k]];
             std::string cond = lf.cond ? E.ev(order_conjuncts(lf.cond)).c : "";
+            allconds += cond;
             std::string ind = cond.empty() ? "    " : "        ";
             if (!cond.empty()) upd << "    if (" << cond << ") {\n";
             for (size_t j = k; j < act.size(); j++) {
@@ -1444,11 +1477,17 @@ private:
             }
             if (!cond.empty()) upd << "    }\n";
         }
+        std::string updates = upd.str();
+        std::vector<std::string> dcls(E.decls.begin(), E.decls.end());
+        std::vector<std::string*> pieces{&rowcond, &updates};
+        for (auto& d : dcls) pieces.push_back(&d);
+        std::string condtext = rowcond + allconds;
+        std::string hoisted = hoist_row_loads(condtext, pieces);
         row << "RF_DEV void rf_row(const RfParams& P, long long r, RfAcc& A)\n{\n";
-        row << body.str();
-        for (auto& dcl : E.decls) row << "    " << dcl << "\n";
+        row << body.str() << hoisted;
+        for (auto& dcl : dcls) row << "    " << dcl << "\n";
         row << "    if (!(" << rowcond << ")) return;\n";
-        row << upd.str();
+        row << updates;
         if (act.empty()) row << "    (void)A;\n";
         row << "}\n\n";
 
@@ -1553,8 +1592,13 @@ private:
             for (size_t i = 1; i < filters.size(); i++) f = reffiner::_and(f, filters[i]);
             filt = E.ev(order_conjuncts(f)).c;
         }
+        std::string gconds = filt;
         gb << "    if (!(" << filt << ")) return -1;\n";
-        for (size_t k = 0; k < key_exprs.size(); k++) gb << "    const auto key" << k << " = " << E.ev(key_exprs[k]).c << ";\n";
+        for (size_t k = 0; k < key_exprs.size(); k++) {
+            std::string kc = E.ev(key_exprs[k]).c;
+            gconds += kc;
+            gb << "    const auto key" << k << " = " << kc << ";\n";
+        }
         gb << "    int g = -1;\n";
         for (int g = 0; g < G; g++) {
             auto& lf = leaves[groups[g][0]];
@@ -1575,11 +1619,16 @@ private:
             gb << "    V.v" << m << " = " << val << ";\n";
         }
         gb << "    return g;\n";
+        std::string gbody = gb.str();
+        std::vector<std::string> dcls(E.decls.begin(), E.decls.end());
+        std::vector<std::string*> pieces{&rowcond, &gbody};
+        for (auto& dd : dcls) pieces.push_back(&dd);
+        std::string hoisted = hoist_row_loads(rowcond + gconds, pieces);
         o << "RF_DEV int rf_group(const RfParams& P, long long r, RfVals& V)\n{\n";
-        o << body.str();
-        for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+        o << body.str() << hoisted;
+        for (auto& dcl : dcls) o << "    " << dcl << "\n";
         o << "    if (!(" << rowcond << ")) return -1;\n";
-        o << gb.str() << "}\n\n";
+        o << gbody << "}\n\n";
 
         // epilogue
         Emitter Ef(*this);
