@@ -62,6 +62,8 @@ typedef struct RfParams {
     void* aux1;
     void* aux2;
     void* aux3;
+    void* aux4;
+    void* aux5;
     long long aux_n0, aux_n1;  // kernel-specific sizes
     int nunits;                // work units (virtual CTAs) of the reduction
     int flags;

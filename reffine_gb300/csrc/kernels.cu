@@ -75,3 +75,91 @@ extern "C" int rf_k_index_build(const void* keys, const unsigned short* valid, l
                                                                  cap, special, err);
     return (int)cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------------------
+// Exclusive prefix sum of n int64 values, in place; data[n] receives the total.
+// Three launches: per-block sums, a one-block scan of those sums, per-block scans plus offset.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kScanT = 1024;
+constexpr int kScanPer = 2 * kScanT;
+
+__device__ long long block_incl_scan(long long x, long long* wsum)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        long long y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        long long w = wsum[lane];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        wsum[lane] = w;
+    }
+    __syncthreads();
+    long long r = x + (warp ? wsum[warp - 1] : 0);
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanT) scan_sums_kernel(const long long* data, long long n, long long* sums)
+{
+    __shared__ long long wsum[32];
+    long long base = (long long)blockIdx.x * kScanPer;
+    long long a = base + 2 * threadIdx.x;
+    long long v = (a < n ? data[a] : 0) + (a + 1 < n ? data[a + 1] : 0);
+    long long s = block_incl_scan(v, wsum);
+    if (threadIdx.x == kScanT - 1) sums[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kScanT) scan_top_kernel(long long* sums, long long nb)
+{
+    __shared__ long long wsum[32];
+    __shared__ long long carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (long long b = 0; b < nb; b += kScanT) {
+        long long i = b + threadIdx.x;
+        long long v = i < nb ? sums[i] : 0;
+        long long s = block_incl_scan(v, wsum);
+        if (i < nb) sums[i] = carry + s - v;
+        __syncthreads();
+        if (threadIdx.x == kScanT - 1) carry += s;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+__global__ void __launch_bounds__(kScanT) scan_apply_kernel(long long* data, long long n, const long long* sums,
+                                                            long long nb)
+{
+    __shared__ long long wsum[32];
+    long long base = (long long)blockIdx.x * kScanPer;
+    long long a = base + 2 * threadIdx.x;
+    long long v0 = a < n ? data[a] : 0, v1 = a + 1 < n ? data[a + 1] : 0;
+    long long s = block_incl_scan(v0 + v1, wsum);
+    long long off = sums[blockIdx.x] + s - (v0 + v1);
+    if (a < n) data[a] = off;
+    if (a + 1 < n) data[a + 1] = off + v0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) data[n] = sums[nb];
+}
+
+}  // namespace
+
+extern "C" int rf_k_scan_excl(long long* data, long long n, long long* tmp, cudaStream_t stream)
+{
+    long long nb = (n + kScanPer - 1) / kScanPer;
+    if (nb < 1) nb = 1;
+    scan_sums_kernel<<<(unsigned)nb, kScanT, 0, stream>>>(data, n, tmp);
+    scan_top_kernel<<<1, kScanT, 0, stream>>>(tmp, nb);
+    scan_apply_kernel<<<(unsigned)nb, kScanT, 0, stream>>>(data, n, tmp, nb);
+    return (int)cudaGetLastError();
+}

@@ -11,6 +11,10 @@ extern "C" {
 int rf_k_index_build(const void* keys, const unsigned short* valid, long long n, long long* slots,
                      unsigned long long cap, long long* special, int* err, cudaStream_t stream);
 
+// Exclusive prefix sum of n int64 values in place (3 launches); data must hold n+1 entries, the
+// last receives the total.  tmp must hold ceil(n / 2048) + 1 entries.
+int rf_k_scan_excl(long long* data, long long n, long long* tmp, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -425,8 +425,12 @@ private:
             return scalar(nm + "()", t);
         }
 
+        std::map<const ExprNode*, Val> node_bind;  // precomputed values of non-symbol nodes (Reduce)
+
         Val ev(const Expr& e)
         {
+            auto nb = node_bind.find(e.get());
+            if (nb != node_bind.end()) return nb->second;
             switch (e->kind) {
                 case NodeKind::SYM: {
                     if (auto b = lookup(e.get())) return *b;
@@ -1405,15 +1409,10 @@ private:
         return r;
     }
 
-    void gen_scan_reduce(std::ostringstream& src, const Reduce& red, const Drive& d, std::vector<Leaf>& leaves)
+    // RfAcc (one 8-byte slot per active leaf), rf_acc_init, rf_acc_combine, rf_acc_shfl
+    void emit_acc(std::ostringstream& src, std::vector<Leaf>& leaves, const std::vector<int>& act)
     {
-        plan_.kind = PlanKind::SCAN_REDUCE;
-        const int T = plan_.threads;
-        // accumulator struct: one 8-byte slot per active leaf
-        std::ostringstream acc, init, comb, shfl, row, fin;
-        std::vector<int> act;
-        for (size_t i = 0; i < leaves.size(); i++)
-            if (leaves[i].op != AggOp::NONE) act.push_back((int)i);
+        std::ostringstream acc, init, comb, shfl;
         Emitter Ei(*this);
         bind_inputs(Ei);
         acc << "struct RfAcc {\n";
@@ -1444,8 +1443,14 @@ private:
         for (size_t k = 0; k < act.size(); k++) shfl << "    R.a" << k << " = __shfl_down_sync(0xffffffffu, A.a" << k << ", off);\n";
         if (act.empty()) shfl << "    R.unused = A.unused; (void)off;\n";
         shfl << "    return R;\n}\n\n";
+        src << acc.str() << init.str() << comb.str() << shfl.str();
+    }
 
-        // row function
+    // rf_row: one row of the driving loop folded into the accumulator
+    void emit_row(std::ostringstream& src, const Reduce& red, const Drive& d, std::vector<Leaf>& leaves,
+                  const std::vector<int>& act)
+    {
+        std::ostringstream row;
         Emitter E(*this);
         std::ostringstream body;
         std::string rowcond = bind_row(E, red, d, body);
@@ -1490,6 +1495,19 @@ private:
         row << updates;
         if (act.empty()) row << "    (void)A;\n";
         row << "}\n\n";
+        src << row.str();
+    }
+
+    void gen_scan_reduce(std::ostringstream& src, const Reduce& red, const Drive& d, std::vector<Leaf>& leaves)
+    {
+        plan_.kind = PlanKind::SCAN_REDUCE;
+        const int T = plan_.threads;
+        std::vector<int> act;
+        for (size_t i = 0; i < leaves.size(); i++)
+            if (leaves[i].op != AggOp::NONE) act.push_back((int)i);
+        emit_acc(src, leaves, act);
+        emit_row(src, red, d, leaves, act);
+        std::ostringstream fin;
 
         // epilogue
         Emitter Ef(*this);
@@ -1509,7 +1527,7 @@ private:
         for (auto& dcl : Ef.decls) fin << "    " << dcl << "\n";
         fin << fb.str() << stores.str() << "}\n\n";
 
-        src << acc.str() << init.str() << comb.str() << shfl.str() << row.str() << fin.str();
+        src << fin.str();
         src << "#define RF_SCAN_REDUCE 1\n#include \"rf_templates.cuh\"\n";
         src << "RF_SCAN_REDUCE_KERNEL(rf_main, " << T << ")\n";
         plan_.kernels.push_back({"rf_main", T, 0, KernelSpec::MAIN});
@@ -1718,6 +1736,68 @@ private:
         }
     }
 
+    // Segmented reduce over run-end encoded rows: every run is cut into chunks of RF_SEG_CH rows
+    // (long Zipf runs spread over many threads); chunk c of run r is reduced by one thread in row
+    // order into partial[woff[r] + c]; the element functions fold a run's partials in order.
+    // woff: (long long*)P.aux4 (nruns + 1 entries), partials: (RfAcc*)P.aux5.
+    void emit_seg_kernels(std::ostringstream& o, const Drive& d)
+    {
+        std::string c0 = "P.t[" + std::to_string(d.slot) + "].col[0]";
+        o << "#define RF_SEG_CH 256\n";
+        o << "extern \"C\" __global__ void __launch_bounds__(256) rf_seg_count(const __grid_constant__ RfParams P)\n{\n";
+        o << "    long long* woff = (long long*)P.aux4;\n    const long long n = " << c0 << ".len;\n";
+        o << "    for (long long run = blockIdx.x * (long long)blockDim.x + threadIdx.x; run < n; run += (long long)gridDim.x * blockDim.x) {\n";
+        o << "        long long len = rf_runend(" << c0 << ", run) - rf_runend(" << c0 << ", run - 1);\n";
+        o << "        long long c = (len + RF_SEG_CH - 1) / RF_SEG_CH;\n        woff[run] = c < 1 ? 1 : c;\n    }\n}\n\n";
+        o << "extern \"C\" __global__ void __launch_bounds__(256) rf_seg_reduce(const __grid_constant__ RfParams P)\n{\n";
+        o << "    const long long* woff = (const long long*)P.aux4;\n    RfAcc* part = (RfAcc*)P.aux5;\n";
+        o << "    const long long n = " << c0 << ".len, W = woff[n];\n";
+        o << "    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < W; w += (long long)gridDim.x * blockDim.x) {\n";
+        o << "        long long lo = 0, hi = n;  // last run with woff[run] <= w\n";
+        o << "        while (hi - lo > 1) { long long mid = (lo + hi) >> 1; if (woff[mid] <= w) lo = mid; else hi = mid; }\n";
+        o << "        const long long run = lo, k = w - woff[run];\n";
+        o << "        const long long s = rf_runend(" << c0 << ", run - 1) + k * RF_SEG_CH;\n";
+        o << "        long long e = rf_runend(" << c0 << ", run);\n        if (e > s + RF_SEG_CH) e = s + RF_SEG_CH;\n";
+        o << "        RfAcc A;\n        rf_acc_init(P, A);\n        for (long long r = s; r < e; r++) rf_row(P, r, A);\n";
+        o << "        rf_st_words(part + w, &A, (int)sizeof(RfAcc));\n    }\n}\n\n";
+        o << "RF_DEV void rf_fold(const RfParams& P, long long run, RfAcc& A)\n{\n";
+        o << "    const long long* woff = (const long long*)P.aux4;\n    const RfAcc* part = (const RfAcc*)P.aux5;\n";
+        o << "    rf_acc_init(P, A);\n    for (long long w = woff[run]; w < woff[run + 1]; w++) {\n";
+        o << "        RfAcc p;\n        rf_ld_words(&p, part + w, (int)sizeof(RfAcc));\n        rf_acc_combine(A, p);\n    }\n}\n\n";
+        plan_.kernels.push_back({"rf_seg_count", 256, 0, KernelSpec::SEGCOUNT});
+        plan_.kernels.push_back({"", 0, 0, KernelSpec::SEGSCAN});
+        plan_.kernels.push_back({"rf_seg_reduce", 256, 0, KernelSpec::SEGREDUCE});
+    }
+
+    // the final state of a folded accumulator `SA`, as a struct value
+    Val seg_state(Emitter& E, std::ostringstream& body, const Reduce& red, std::vector<Leaf>& leaves)
+    {
+        std::map<std::vector<size_t>, std::string> finals;
+        for (size_t i = 0, k = 0; i < leaves.size(); i++) {
+            auto& lf = leaves[i];
+            std::string tot = lf.op == AggOp::NONE ? "0" : "SA.a" + std::to_string(k++);
+            std::string nm = "sst" + std::to_string(i);
+            body << "    const " << ctype(lf.type) << " " << nm << " = " << final_leaf(E, lf, tot) << ";\n";
+            finals[lf.path] = nm;
+        }
+        std::function<Val(const DataType&, std::vector<size_t>)> mk = [&](const DataType& t, std::vector<size_t> pth) {
+            Val v;
+            v.type = t;
+            if (t.is_struct()) {
+                v.k = Val::STRUCT;
+                for (size_t i = 0; i < t.dtypes.size(); i++) {
+                    auto q = pth;
+                    q.push_back(i);
+                    v.f.push_back(mk(t.dtypes[i], q));
+                }
+                return v;
+            }
+            v.c = finals.at(pth);
+            return v;
+        };
+        return mk(red.type, {});
+    }
+
     void lower_op(const Expr& opx)
     {
         const Op& op = *as<Op>(opx);
@@ -1738,11 +1818,60 @@ private:
         src << "// generated by the reffine_gb300 lowering pass: " << fn_->name << " (Op materialisation)\n";
         src << "#include \"rf_device.cuh\"\n\n";
         emit_range_kernels(src, d);
+
+        // an Op over a 2-d vector whose outputs reduce each element's sub-vector
+        // (LoopGen::visit(Element) dim 2 -> SubVector of run ends, loopgen.cpp:34-38)
+        const Reduce* seg = nullptr;
+        std::vector<Leaf> seg_leaves;
+        std::vector<int> seg_act;
+        if (d.sp.has_vec && fn_->inputs[d.input]->type.dim == 2) {
+            std::vector<const Reduce*> reds;
+            for (auto& o : op.outputs) find_reduces(o, reds);
+            for (auto& f : d.sp.filters) find_reduces(f, reds);
+            std::sort(reds.begin(), reds.end());
+            reds.erase(std::unique(reds.begin(), reds.end()), reds.end());
+            if (reds.size() > 1) throw LowerError("more than one nested Reduce per element");
+            if (reds.size() == 1) {
+                seg = reds[0];
+                if (seg->vec->kind != NodeKind::ELEMENT) throw LowerError("nested Reduce over a non-element vector");
+                auto el = as<Element>(seg->vec);
+                if (resolve(el->vec).get() != resolve(d.sp.vec_node).get() || el->iter.get() != op.iters[0].get())
+                    throw LowerError("nested Reduce over another vector's element");
+                const DataType& vt = fn_->inputs[d.input]->type;
+                if (vt.encodings[0] != RUNEND)
+                    throw LowerError("grouped Op over a flat key column: lowered by the hash group-by template");
+                plan_.kind = PlanKind::SEG_REDUCE;
+                collect_leaves(*seg, seg->type, {}, seg_leaves);
+                for (size_t i = 0; i < seg_leaves.size(); i++)
+                    if (seg_leaves[i].op != AggOp::NONE) seg_act.push_back((int)i);
+                emit_acc(src, seg_leaves, seg_act);
+                plan_.acc_bytes = std::max<size_t>(8, seg_act.size() * 8);
+                Drive rd;
+                rd.subvec = true;
+                rd.input = d.input;
+                rd.slot = d.slot;
+                emit_row(src, *seg, rd, seg_leaves, seg_act);
+                emit_seg_kernels(src, d);
+            }
+        }
+        auto bind_seg = [&](Emitter& E, std::ostringstream& body) {
+            if (!seg) return;
+            body << "    RfAcc SA;\n    rf_fold(P, r, SA);\n";
+            Val st = seg_state(E, body, *seg, seg_leaves);
+            E.node_bind[(const ExprNode*)seg] = st;
+        };
         {
             Emitter E(*this);
             bind_inputs(E);
             std::ostringstream body;
             std::string cond = bind_op_row(E, op, d, body);
+            bool needs = false;
+            for (auto& f : d.sp.filters) {
+                std::vector<const Reduce*> rr;
+                find_reduces(f, rr);
+                needs |= !rr.empty();
+            }
+            if (needs) bind_seg(E, body);
             src << "RF_DEV bool rf_cond(const RfParams& P, long long r)\n{\n" << body.str();
             for (auto& dcl : E.decls) src << "    " << dcl << "\n";
             src << "    return " << cond << ";\n}\n\n";
@@ -1752,6 +1881,7 @@ private:
             bind_inputs(E);
             std::ostringstream body;
             bind_op_row(E, op, d, body);
+            bind_seg(E, body);
             std::ostringstream w;
             size_t c = 0;
             for (auto& i : op.iters) {

@@ -53,7 +53,7 @@ struct KernelSpec {
     std::string name;
     int threads = 256;
     size_t smem = 0;
-    enum Role { MAIN, RANGE, STOP, COUNT, SCAN, SCATTER, INIT, FINAL } role = MAIN;
+    enum Role { MAIN, RANGE, STOP, COUNT, SCAN, SCATTER, INIT, FINAL, SEGCOUNT, SEGSCAN, SEGREDUCE } role = MAIN;
 };
 
 struct Plan {
@@ -78,7 +78,8 @@ struct Plan {
     DataType out_type;
     size_t out_size = 0;                // bytes of the value output (C layout)
     bool out_is_table = false;
-    size_t acc_bytes = 0;               // bytes of one unit's partial (scan-reduce)
+    size_t acc_bytes = 0;               // bytes of one unit's partial (scan-reduce, segmented reduce)
+    int seg_chunk = 256;                // segmented reduce: rows per chunk
     int groups = 0, aggs = 0;           // grouped plans
     std::vector<DataType> out_cols;     // table outputs: column types
     int out_dim = 0;

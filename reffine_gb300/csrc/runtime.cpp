@@ -150,7 +150,29 @@ struct rf_plan {
     long long* d_tiles = nullptr;     // per-tile counts / offsets
     size_t tiles_cap = 0;
     long long* d_res = nullptr;       // [rows written, null count]
+    // segmented reduce
+    long long* seg_woff = nullptr;
+    long long* seg_tmp = nullptr;
+    void* seg_part = nullptr;
+    size_t seg_runs_cap = 0, seg_part_cap = 0;
 };
+
+namespace {
+// grows a device buffer to at least `bytes` (contents not kept)
+bool grow(void** buf, size_t* cap, size_t bytes, cudaStream_t s)
+{
+    if (*buf && *cap >= bytes) return true;
+    if (*buf) {
+        cudaStreamSynchronize(s);
+        cudaFree(*buf);
+    }
+    *buf = nullptr;
+    *cap = 0;
+    if (cudaMalloc(buf, bytes) != cudaSuccess) return false;
+    *cap = bytes;
+    return true;
+}
+}  // namespace
 
 // ------------------------------------------------------------------------------------------
 // helpers
@@ -822,7 +844,11 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
     int rc = jit_compile(ctx, p->plan.key, p->plan.source, p->mod, nullptr);
     if (rc) return rc;
     for (auto& k : p->plan.kernels) {
-        CUfunction f;
+        CUfunction f = nullptr;
+        if (k.name.empty()) {  // a step run by the library's own kernels (kernels.cu)
+            p->fns.push_back(nullptr);
+            continue;
+        }
         if ((rc = get_function(ctx, *p->mod, k.name, f))) return rc;
         if (k.smem > 48 * 1024) {
             CUresult cr = drv().FuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)k.smem);
@@ -896,6 +922,9 @@ extern "C" int rf_plan_free(rf_plan* p)
     cudaFree(p->d_ptrs);
     cudaFree(p->d_tiles);
     cudaFree(p->d_res);
+    cudaFree(p->seg_woff);
+    cudaFree(p->seg_tmp);
+    cudaFree(p->seg_part);
     for (auto* t : p->staging)
         if (t) {
             free_table_mem(t);
@@ -1121,11 +1150,38 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     P.aux1 = p->d_ptrs + RF_MAX_COLS;
     P.aux2 = p->d_tiles;
     P.aux3 = p->d_res;
+    long long nruns = 0;
+    if (pl.kind == rfg::PlanKind::SEG_REDUCE) {
+        rf_table* vt = args[pl.drive_input].table;
+        nruns = vt->cols[0].nvals;
+        long long nrows = vt->cols[0].logical;
+        size_t wmax = (size_t)(nruns + (nrows + pl.seg_chunk - 1) / pl.seg_chunk + 2);
+        size_t cap1 = 0;
+        if (!grow((void**)&p->seg_woff, &p->seg_runs_cap, (size_t)(nruns + 2) * 8, s) ||
+            !grow((void**)&p->seg_tmp, &cap1, (size_t)(nruns / 2048 + 4) * 8, s) ||
+            !grow(&p->seg_part, &p->seg_part_cap, wmax * pl.acc_bytes, s)) {
+            free_table_mem(t.get());
+            return fail(ctx, RF_ERR_OOM, "segmented-reduce buffers");
+        }
+        P.aux4 = p->seg_woff;
+        P.aux5 = p->seg_part;
+    }
     int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
     P.nunits = units;
     for (size_t i = 0; i < pl.kernels.size(); i++) {
         const auto& k = pl.kernels[i];
+        if (k.role == rfg::KernelSpec::SEGSCAN) {
+            int e = rf_k_scan_excl(p->seg_woff, nruns, p->seg_tmp, s);
+            if (e) {
+                free_table_mem(t.get());
+                return fail(ctx, RF_ERR_CUDA, "segment scan launch: %s", cudaGetErrorString((cudaError_t)e));
+            }
+            ctx->launches += 3;
+            continue;
+        }
         int grid = units;
+        if (k.role == rfg::KernelSpec::SEGCOUNT || k.role == rfg::KernelSpec::SEGREDUCE)
+            grid = ctx->sm_count * 8;
         if (k.role == rfg::KernelSpec::RANGE || k.role == rfg::KernelSpec::SCAN) grid = 1;
         if (k.role == rfg::KernelSpec::STOP)
             grid = (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8);
