@@ -195,6 +195,43 @@ RF_DEV void rf_ld_words(void* dst, const void* src, int nbytes)
     for (int i = 0; i < nbytes / 8; i++) d[i] = __ldcg(s + i);
 }
 
+// ---------------------------------------------------------------------------------------
+// atomic accumulate of one aggregate into a 64-bit slot (shared or global memory)
+// ---------------------------------------------------------------------------------------
+RF_DEV void rf_atom_fsum(unsigned long long* p, double v) { atomicAdd((double*)p, v); }
+RF_DEV void rf_atom_isum(unsigned long long* p, long long v) { atomicAdd(p, (unsigned long long)v); }
+RF_DEV void rf_atom_imax(unsigned long long* p, long long v) { atomicMax((long long*)p, v); }
+RF_DEV void rf_atom_imin(unsigned long long* p, long long v) { atomicMin((long long*)p, v); }
+RF_DEV void rf_atom_umax(unsigned long long* p, unsigned long long v) { atomicMax(p, v); }
+RF_DEV void rf_atom_umin(unsigned long long* p, unsigned long long v) { atomicMin(p, v); }
+RF_DEV void rf_atom_or(unsigned long long* p, long long v) { if (v) atomicOr(p, 1ULL); }
+RF_DEV void rf_atom_and(unsigned long long* p, long long v) { if (!v) atomicAnd(p, 0ULL); }
+// binary64 max/min with std::max/std::min semantics, by compare-and-swap (bounded retries)
+RF_DEV bool rf_atom_fmax(unsigned long long* p, double v)
+{
+    unsigned long long old = *(volatile unsigned long long*)p;
+    for (int i = 0; i < (1 << 20); i++) {
+        double cur = __longlong_as_double((long long)old);
+        if (!(cur < v)) return true;
+        unsigned long long prev = atomicCAS(p, old, (unsigned long long)__double_as_longlong(v));
+        if (prev == old) return true;
+        old = prev;
+    }
+    return false;
+}
+RF_DEV bool rf_atom_fmin(unsigned long long* p, double v)
+{
+    unsigned long long old = *(volatile unsigned long long*)p;
+    for (int i = 0; i < (1 << 20); i++) {
+        double cur = __longlong_as_double((long long)old);
+        if (!(v < cur)) return true;
+        unsigned long long prev = atomicCAS(p, old, (unsigned long long)__double_as_longlong(v));
+        if (prev == old) return true;
+        old = prev;
+    }
+    return false;
+}
+
 // 64-bit slot encodings
 RF_DEV unsigned long long rf_f2u(double x) { return (unsigned long long)__double_as_longlong(x); }
 RF_DEV double rf_u2f(unsigned long long x) { return __longlong_as_double((long long)x); }

@@ -163,3 +163,44 @@ extern "C" int rf_k_scan_excl(long long* data, long long n, long long* tmp, cuda
     scan_apply_kernel<<<(unsigned)nb, kScanT, 0, stream>>>(data, n, tmp, nb);
     return (int)cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------------------
+// Distinct-count sketch of an int64 column: HyperLogLog (Flajolet, Fusy, Gandouet, Meunier,
+// 2007) with 2^14 registers, used to size hash tables.  Register j holds the largest rank
+// (leading zeros + 1) of the hashed keys whose top 14 bits are j.  Registers are kept per block
+// in shared memory (a register is only written when its value grows) and merged with atomicMax.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kHllBits = 14;
+constexpr int kHllM = 1 << kHllBits;
+
+__global__ void __launch_bounds__(512) hll_kernel(const long long* __restrict__ keys, const unsigned short* __restrict__ valid,
+                                                  long long n, unsigned* regs)
+{
+    __shared__ unsigned r[kHllM];
+    for (int i = threadIdx.x; i < kHllM; i += blockDim.x) r[i] = 0;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (!rf_valid(valid, i)) continue;
+        unsigned long long h = rf_mix64((unsigned long long)__ldg(keys + i));
+        unsigned j = (unsigned)(h >> (64 - kHllBits));
+        unsigned long long w = (h << kHllBits) | (1ULL << (kHllBits - 1));
+        unsigned rank = (unsigned)__clzll((long long)w) + 1u;
+        if (rank > r[j]) atomicMax(&r[j], rank);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kHllM; i += blockDim.x)
+        if (r[i]) atomicMax(&regs[i], r[i]);
+}
+
+}  // namespace
+
+extern "C" int rf_k_hll(const void* keys, const unsigned short* valid, long long n, unsigned* regs, cudaStream_t stream)
+{
+    cudaMemsetAsync(regs, 0, sizeof(unsigned) * kHllM, stream);
+    int blocks = grid_for(n, 512);
+    if (blocks > 152 * 2) blocks = 152 * 2;
+    hll_kernel<<<blocks, 512, 0, stream>>>(static_cast<const long long*>(keys), valid, n, regs);
+    return (int)cudaGetLastError();
+}

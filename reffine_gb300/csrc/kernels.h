@@ -15,6 +15,10 @@ int rf_k_index_build(const void* keys, const unsigned short* valid, long long n,
 // last receives the total.  tmp must hold ceil(n / 2048) + 1 entries.
 int rf_k_scan_excl(long long* data, long long n, long long* tmp, cudaStream_t stream);
 
+// HyperLogLog registers (2^14 unsigned, device) of an int64 column (2 launches).
+#define RF_HLL_M 16384
+int rf_k_hll(const void* keys, const unsigned short* valid, long long n, unsigned* regs, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1798,6 +1798,266 @@ private:
         return mk(red.type, {});
     }
 
+    // Hash group-by: the grouped Op over a 2-d vector whose key column (column 0) is flat and
+    // unsorted.  The groups are the distinct valid keys - the runs the reference would see after
+    // sorting and run-end encoding - so each output row is the same; rows come out in slot order.
+    //   rf_hg_init  fills the table: keys RF_EMPTY_KEY, accumulators at their identity
+    //   rf_hg_agg   one pass over the rows: a per-block shared-memory table pre-aggregates the
+    //               frequent keys, the rest go to the global open-addressing table (load 0.5)
+    //   rf_cond / rf_emit   the materialisation template over the slots
+    // Device layout: keys (long long*)P.aux4 [C + 1] (slot C: the key RF_EMPTY_KEY itself, used
+    // flag in its key word), accumulators (unsigned long long*)P.aux5 [L][C + 1], rows P.aux_n0,
+    // capacity C = P.aux_n1.
+    void lower_hash_group(const Op& op, const Drive& d, const Reduce& red)
+    {
+        plan_.kind = PlanKind::HASH_GROUP;
+        const int T = plan_.threads;
+        std::vector<Leaf> leaves;
+        collect_leaves(red, red.type, {}, leaves);
+        std::vector<int> act;
+        for (size_t i = 0; i < leaves.size(); i++)
+            if (leaves[i].op != AggOp::NONE) act.push_back((int)i);
+        const int L = (int)act.size();
+        const int S = std::max(256, std::min(2048, (int)(96 * 1024 / (8 * (L + 1)))));
+        std::string sl = std::to_string(d.slot);
+        std::string c0 = "P.t[" + sl + "].col[0]";
+        std::ostringstream o;
+        o << "// generated by the reffine_gb300 lowering pass: " << fn_->name << " (hash group-by)\n";
+        o << "#include \"rf_device.cuh\"\n\n#define RF_HG_L " << std::max(L, 1) << "\n#define RF_HG_S " << S << "\n\n";
+        auto kind_of = [&](const Leaf& lf) -> std::string {
+            bool f = lf.type.is_float() && !lf.count;
+            switch (lf.op) {
+                case AggOp::SUM: return f ? "fsum" : "isum";
+                case AggOp::MAX: return f ? "fmax" : (lf.type.is_unsigned() ? "umax" : "imax");
+                case AggOp::MIN: return f ? "fmin" : (lf.type.is_unsigned() ? "umin" : "imin");
+                case AggOp::OR: return "or";
+                case AggOp::AND: return "and";
+                default: return "none";
+            }
+        };
+        auto enc = [&](const Leaf& lf, const std::string& x) -> std::string {
+            if (lf.type.is_float() && !lf.count) return "rf_f2u((double)(" + x + "))";
+            return "(unsigned long long)(long long)(" + x + ")";
+        };
+        auto arg = [&](const Leaf& lf, const std::string& raw) -> std::string {
+            if (lf.type.is_float() && !lf.count) return "rf_u2f(" + raw + ")";
+            if (kind_of(lf) == "umax" || kind_of(lf) == "umin") return raw;
+            return "(long long)(" + raw + ")";
+        };
+        // identities
+        {
+            Emitter Ei(*this);
+            bind_inputs(Ei);
+            std::ostringstream b;
+            for (int k = 0; k < L; k++) {
+                auto& lf = leaves[act[k]];
+                std::string v = lf.op == AggOp::SUM ? "0ULL" : enc(lf, "(" + acc_ctype(lf) + ")(" + Ei.ev(lf.init).c + ")");
+                b << "    case " << k << ": return " << v << ";\n";
+            }
+            o << "RF_DEV unsigned long long rf_hg_identity(const RfParams& P, int l)\n{\n";
+            for (auto& dcl : Ei.decls) o << "    " << dcl << "\n";
+            o << "    switch (l) {\n" << b.str() << "    default: return 0ULL;\n    }\n}\n\n";
+        }
+        // one row's contribution to the accumulators of its group (slot A, leaf stride `st`)
+        {
+            Emitter E(*this);
+            bind_inputs(E);
+            const DataType& vt = fn_->inputs[d.input]->type;
+            Val v;
+            v.k = Val::STRUCT;
+            v.type = red.val->type;
+            for (size_t c = 1; c < vt.dtypes.size(); c++)
+                v.f.push_back(E.scalar("rf_ld<" + ctype(vt.dtypes[c]) + ">(P.t[" + sl + "].col[" + std::to_string(c) + "].data, r)",
+                                       vt.dtypes[c]));
+            E.bind(red.val, v);
+            std::ostringstream u;
+            for (int k = 0; k < L; k++) {
+                auto& lf = leaves[act[k]];
+                std::string cond = lf.cond ? E.ev(order_conjuncts(lf.cond)).c : "";
+                std::string val = lf.count ? "1" : "(" + acc_ctype(lf) + ")(" + E.ev(lf.value).c + ")";
+                std::string call = "rf_atom_" + kind_of(lf) + "(A + " + std::to_string(k) + " * st, " + val + ")";
+                if (kind_of(lf) == "fmax" || kind_of(lf) == "fmin") call = "if (!" + call + ") rf_set_err(P, RF_DEVERR_WAIT)";
+                if (!cond.empty()) u << "    if (" << cond << ") { " << call << "; }\n";
+                else u << "    " << call << ";\n";
+            }
+            o << "RF_DEV void rf_hg_apply(const RfParams& P, long long r, unsigned long long* A, long long st)\n{\n";
+            for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+            o << "    if (!rf_valid(P.t[" << sl << "].col[1].valid, r)) return;  // loopgen.cpp:238\n";
+            o << u.str() << "    (void)A; (void)st;\n}\n\n";
+        }
+        // flush of a pre-aggregated slot into the global table
+        o << "RF_DEV void rf_hg_merge(const RfParams& P, unsigned long long* A, long long st, const unsigned long long* B, long long bst)\n{\n";
+        for (int k = 0; k < L; k++) {
+            auto& lf = leaves[act[k]];
+            std::string raw = "B[" + std::to_string(k) + " * bst]";
+            std::string call = "rf_atom_" + kind_of(lf) + "(A + " + std::to_string(k) + " * st, " + arg(lf, raw) + ")";
+            if (kind_of(lf) == "fmax" || kind_of(lf) == "fmin") call = "if (!" + call + ") rf_set_err(P, RF_DEVERR_WAIT)";
+            o << "    " << call << ";\n";
+        }
+        o << "    (void)A; (void)B; (void)st; (void)bst;\n}\n\n";
+        o << R"(// slot of `key` in the global table (claimed if new); C + 1 slots, slot C is the empty key's
+RF_DEV long long rf_hg_slot(const RfParams& P, long long key)
+{
+    long long* keys = (long long*)P.aux4;
+    const unsigned long long C = (unsigned long long)P.aux_n1;
+    if (key == RF_EMPTY_KEY) {
+        if (keys[C] == 0) atomicExch((unsigned long long*)(keys + C), 1ULL);
+        return (long long)C;
+    }
+    unsigned long long h = rf_home(key, C);
+    for (unsigned long long n = 0; n < C; ++n) {
+        unsigned long long old = atomicCAS((unsigned long long*)(keys + h), (unsigned long long)RF_EMPTY_KEY,
+                                           (unsigned long long)key);
+        if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) return (long long)h;
+        if (++h == C) h = 0;
+    }
+    rf_set_err(P, RF_DEVERR_OVERFLOW);
+    return -1;
+}
+
+extern "C" __global__ void __launch_bounds__(256) rf_hg_init(const __grid_constant__ RfParams P)
+{
+    long long* keys = (long long*)P.aux4;
+    unsigned long long* acc = (unsigned long long*)P.aux5;
+    const long long C = P.aux_n1;
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s <= C; s += (long long)gridDim.x * blockDim.x) {
+        keys[s] = s < C ? RF_EMPTY_KEY : 0;
+        for (int l = 0; l < RF_HG_L; l++) acc[(long long)l * (C + 1) + s] = rf_hg_identity(P, l);
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constant__ RfParams P)
+{
+    __shared__ long long sk[RF_HG_S];
+    __shared__ unsigned long long sv[RF_HG_L * RF_HG_S];
+    for (int i = threadIdx.x; i < RF_HG_S; i += blockDim.x) {
+        sk[i] = RF_EMPTY_KEY;
+        for (int l = 0; l < RF_HG_L; l++) sv[l * RF_HG_S + i] = rf_hg_identity(P, l);
+    }
+    __syncthreads();
+    unsigned long long* acc = (unsigned long long*)P.aux5;
+    const long long C = P.aux_n1, n = P.aux_n0;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+)";
+        o << "        if (!rf_valid(" << c0 << ".valid, r)) continue;  // a null key is no group\n";
+        o << "        const long long key = rf_ld<int64_t>(" << c0 << ".data, r);\n";
+        o << R"(        unsigned long long* A = nullptr;
+        long long st = 0;
+        if (key != RF_EMPTY_KEY) {
+            unsigned h = (unsigned)rf_home(key, RF_HG_S);
+            for (int p = 0; p < 8; p++) {
+                unsigned long long old = atomicCAS((unsigned long long*)&sk[h], (unsigned long long)RF_EMPTY_KEY,
+                                                   (unsigned long long)key);
+                if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) {
+                    A = sv + h;
+                    st = RF_HG_S;
+                    break;
+                }
+                if (++h == RF_HG_S) h = 0;
+            }
+        }
+        if (!A) {
+            long long g = rf_hg_slot(P, key);
+            if (g < 0) continue;
+            A = acc + g;
+            st = C + 1;
+        }
+        rf_hg_apply(P, r, A, st);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < RF_HG_S; i += blockDim.x) {
+        if (sk[i] == RF_EMPTY_KEY) continue;
+        long long g = rf_hg_slot(P, sk[i]);
+        if (g >= 0) rf_hg_merge(P, acc + g, C + 1, sv + i, RF_HG_S);
+    }
+}
+
+)";
+        // element functions over the slots
+        auto elem = [&](Emitter& E, std::ostringstream& body) {
+            body << "    const long long* keys = (const long long*)P.aux4;\n";
+            body << "    const unsigned long long* acc = (const unsigned long long*)P.aux5;\n";
+            body << "    const long long C = P.aux_n1;\n";
+            body << "    const bool used = r < C ? keys[r] != RF_EMPTY_KEY : keys[C] != 0;\n";
+            body << "    const int64_t it = r < C ? keys[r] : RF_EMPTY_KEY;\n";
+            E.bind(op.iters[0], E.scalar("it", d.sp.iter->type));
+            std::map<std::vector<size_t>, std::string> finals;
+            for (size_t i = 0, k = 0; i < leaves.size(); i++) {
+                auto& lf = leaves[i];
+                std::string tot = "0";
+                if (lf.op != AggOp::NONE) {
+                    std::string raw = "acc[" + std::to_string(k) + " * (C + 1) + r]";
+                    tot = (lf.type.is_float() && !lf.count) ? "rf_u2f(" + raw + ")" : "(long long)(" + raw + ")";
+                    k++;
+                }
+                std::string nm = "hst" + std::to_string(i);
+                body << "    const " << ctype(lf.type) << " " << nm << " = " << final_leaf(E, lf, tot) << ";\n";
+                finals[lf.path] = nm;
+            }
+            std::function<Val(const DataType&, std::vector<size_t>)> mk = [&](const DataType& t, std::vector<size_t> pth) {
+                Val v;
+                v.type = t;
+                if (t.is_struct()) {
+                    v.k = Val::STRUCT;
+                    for (size_t i = 0; i < t.dtypes.size(); i++) {
+                        auto q = pth;
+                        q.push_back(i);
+                        v.f.push_back(mk(t.dtypes[i], q));
+                    }
+                    return v;
+                }
+                v.c = finals.at(pth);
+                return v;
+            };
+            E.node_bind[(const ExprNode*)&red] = mk(red.type, {});
+        };
+        {
+            Emitter E(*this);
+            bind_inputs(E);
+            std::ostringstream body;
+            elem(E, body);
+            std::string cond = "used";
+            for (auto& lb : d.sp.lbs) cond += " && (it >= (int64_t)(" + E.ev(lb).c + "))";
+            for (auto& ub : d.sp.ubs) cond += " && (it <= (int64_t)(" + E.ev(ub).c + "))";
+            for (auto& f : d.sp.filters) cond += " && (" + E.ev(f).c + ")";
+            o << "RF_DEV bool rf_cond(const RfParams& P, long long r)\n{\n" << body.str();
+            for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+            o << "    return " << cond << ";\n}\n\n";
+        }
+        {
+            Emitter E(*this);
+            bind_inputs(E);
+            std::ostringstream body;
+            elem(E, body);
+            std::ostringstream w;
+            size_t c = 0;
+            w << "    ((int64_t*)((void* const*)P.aux0)[" << c++ << "])[o] = it;\n";
+            for (auto& x : op.outputs) {
+                w << "    ((" << ctype(x->type) << "*)((void* const*)P.aux0)[" << c << "])[o] = (" << ctype(x->type) << ")("
+                  << E.ev(x).c << ");\n";
+                c++;
+            }
+            o << "RF_DEV void rf_emit(const RfParams& P, long long r, long long o)\n{\n" << body.str();
+            for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+            o << w.str() << "}\n\n";
+        }
+        if (vectorize_ && !d.sp.filters.empty())
+            throw LowerError("vectorised hash group-by with a filter: validity over groups is not lowered");
+        o << "#define RF_MATERIALIZE 1\n#include \"rf_templates.cuh\"\n";
+        o << "RF_MATERIALIZE_KERNELS(" << T << ", " << plan_.out_cols.size() << ")\n";
+        plan_.kernels.clear();
+        plan_.kernels.push_back({"rf_hg_init", 256, 0, KernelSpec::INIT});
+        plan_.kernels.push_back({"rf_hg_agg", 256, 0, KernelSpec::MAIN});
+        plan_.kernels.push_back({"rf_count", T, 0, KernelSpec::COUNT});
+        plan_.kernels.push_back({"rf_scan", 1024, 0, KernelSpec::SCAN});
+        plan_.kernels.push_back({"rf_scatter", T, 0, KernelSpec::SCATTER});
+        plan_.acc_bytes = (size_t)std::max(L, 1) * 8;
+        plan_.aggs = L;
+        plan_.device_range = false;
+        plan_.source = o.str();
+        if (d.sp.iter->type.btype != INT64) throw LowerError("hash group-by keys must be int64");
+    }
+
     void lower_op(const Expr& opx)
     {
         const Op& op = *as<Op>(opx);
@@ -1838,8 +2098,10 @@ private:
                 if (resolve(el->vec).get() != resolve(d.sp.vec_node).get() || el->iter.get() != op.iters[0].get())
                     throw LowerError("nested Reduce over another vector's element");
                 const DataType& vt = fn_->inputs[d.input]->type;
-                if (vt.encodings[0] != RUNEND)
-                    throw LowerError("grouped Op over a flat key column: lowered by the hash group-by template");
+                if (vt.encodings[0] != RUNEND) {
+                    lower_hash_group(op, d, *seg);
+                    return;
+                }
                 plan_.kind = PlanKind::SEG_REDUCE;
                 collect_leaves(*seg, seg->type, {}, seg_leaves);
                 for (size_t i = 0; i < seg_leaves.size(); i++)

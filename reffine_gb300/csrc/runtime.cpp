@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -130,6 +131,7 @@ struct rf_table {
     bool has_index = false;
     long long null_count = 0;
     std::string name;
+    std::vector<long long> ndv;       // cached distinct-count estimates per column (-1: unknown)
 };
 
 struct rf_plan {
@@ -150,6 +152,11 @@ struct rf_plan {
     long long* d_tiles = nullptr;     // per-tile counts / offsets
     size_t tiles_cap = 0;
     long long* d_res = nullptr;       // [rows written, null count]
+    // hash group-by
+    void* hg_keys = nullptr;
+    void* hg_acc = nullptr;
+    size_t hg_keys_cap = 0, hg_acc_cap = 0;
+    long long hg_retry_cap = 0;
     // segmented reduce
     long long* seg_woff = nullptr;
     long long* seg_tmp = nullptr;
@@ -534,6 +541,7 @@ int upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int6
     t->name = schema->name ? schema->name : "";
     t->has_index = false;
     t->null_count = 0;
+    t->ndv.assign(n, -1);
     t->cols.resize(n);
     t->present.assign(n, 0);
     std::vector<char> want(n, sel ? 0 : 1);
@@ -922,6 +930,8 @@ extern "C" int rf_plan_free(rf_plan* p)
     cudaFree(p->d_ptrs);
     cudaFree(p->d_tiles);
     cudaFree(p->d_res);
+    cudaFree(p->hg_keys);
+    cudaFree(p->hg_acc);
     cudaFree(p->seg_woff);
     cudaFree(p->seg_tmp);
     cudaFree(p->seg_part);
@@ -1088,6 +1098,49 @@ extern "C" int rf_plan_launch(rf_plan* p, const rf_arg* args, int32_t n_args, vo
     return RF_OK;
 }
 
+namespace rfrt {
+
+// Distinct values of an int64 column, estimated with HyperLogLog (kernels.cu) and cached on the
+// table (a table statistic, as a database keeps one; computed once per uploaded table).
+int ndv_estimate(rf_table* t, int col, cudaStream_t s, long long* out)
+{
+    rf_ctx* ctx = t->ctx;
+    if ((int)t->ndv.size() <= col) t->ndv.resize(col + 1, -1);
+    if (t->ndv[col] >= 0) {
+        *out = t->ndv[col];
+        return RF_OK;
+    }
+    DevCol& dc = t->cols[col];
+    unsigned* regs = nullptr;
+    CUDA_TRY(ctx, cudaMalloc((void**)&regs, RF_HLL_M * sizeof(unsigned)));
+    int e = rf_k_hll(dc.data, dc.valid, dc.nvals, regs, s);
+    if (e) {
+        cudaFree(regs);
+        return fail(ctx, RF_ERR_CUDA, "distinct-count sketch launch: %s", cudaGetErrorString((cudaError_t)e));
+    }
+    ctx->launches += 1;
+    std::vector<unsigned> h(RF_HLL_M);
+    cudaError_t ce = cudaMemcpyAsync(h.data(), regs, RF_HLL_M * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    cudaFree(regs);
+    if (ce != cudaSuccess) return fail(ctx, RF_ERR_CUDA, "distinct-count sketch: %s", cudaGetErrorString(ce));
+    double sum = 0, m = RF_HLL_M;
+    int zeros = 0;
+    for (unsigned r : h) {
+        sum += std::ldexp(1.0, -(int)r);
+        zeros += r == 0;
+    }
+    double est = 0.7213 / (1.0 + 1.079 / m) * m * m / sum;
+    if (est <= 2.5 * m && zeros) est = m * std::log(m / zeros);
+    long long v = (long long)(est + 0.5);
+    if (v > dc.nvals) v = dc.nvals;
+    t->ndv[col] = v;
+    *out = v;
+    return RF_OK;
+}
+
+}  // namespace rfrt
+
 namespace {
 
 // Runs an Op plan: allocates the output table (capacity = the loop's row range, so no 1e8-row
@@ -1101,6 +1154,28 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     long long lo, hi;
     int rc = fill_params(p, args, n_args, P, lo, hi);
     if (rc) return rc;
+    long long hg_cap = 0;
+    if (pl.kind == rfg::PlanKind::HASH_GROUP) {
+        // hash table at load factor 0.5 of the estimated distinct keys (10% margin);
+        // a probe overflow reruns with twice the capacity
+        rf_table* vt = args[pl.drive_input].table;
+        long long ndv = 0;
+        if ((rc = ndv_estimate(vt, 0, s, &ndv))) return rc;
+        hg_cap = std::max<long long>(1024, (long long)(2.2 * (double)ndv));
+        if (p->hg_retry_cap > hg_cap) hg_cap = p->hg_retry_cap;
+        size_t L = std::max<size_t>(1, pl.acc_bytes / 8);
+        if (!grow(&p->hg_keys, &p->hg_keys_cap, (size_t)(hg_cap + 1) * 8, s) ||
+            !grow(&p->hg_acc, &p->hg_acc_cap, (size_t)(hg_cap + 1) * 8 * L, s))
+            return fail(ctx, RF_ERR_OOM, "hash table allocation (%lld slots)", hg_cap);
+        P.aux4 = p->hg_keys;
+        P.aux5 = p->hg_acc;
+        P.aux_n0 = vt->cols[0].logical;
+        P.aux_n1 = hg_cap;
+        lo = 0;
+        hi = hg_cap + 1;
+        P.row_lo = lo;
+        P.row_hi = hi;
+    }
     long long cap = hi - lo;
     size_t nc = pl.out_cols.size();
     auto t = std::make_unique<rf_table>();
@@ -1180,8 +1255,10 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
             continue;
         }
         int grid = units;
-        if (k.role == rfg::KernelSpec::SEGCOUNT || k.role == rfg::KernelSpec::SEGREDUCE)
+        if (k.role == rfg::KernelSpec::SEGCOUNT || k.role == rfg::KernelSpec::SEGREDUCE ||
+            k.role == rfg::KernelSpec::INIT)
             grid = ctx->sm_count * 8;
+        if (pl.kind == rfg::PlanKind::HASH_GROUP && k.role == rfg::KernelSpec::MAIN) grid = ctx->sm_count * 2;
         if (k.role == rfg::KernelSpec::RANGE || k.role == rfg::KernelSpec::SCAN) grid = 1;
         if (k.role == rfg::KernelSpec::STOP)
             grid = (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8);
@@ -1197,6 +1274,11 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     rc = check_device_error(ctx);
     if (rc) {
         free_table_mem(t.get());
+        if (pl.kind == rfg::PlanKind::HASH_GROUP && rc == RF_ERR_DEVICE && hg_cap < (1LL << 34) &&
+            ctx->err.find("capacity") != std::string::npos) {
+            p->hg_retry_cap = hg_cap * 2;  // the estimate was low: grow and rerun
+            return run_table(p, args, n_args, out, s);
+        }
         return rc;
     }
     long long rows = res[0];

@@ -117,6 +117,60 @@ def groupby_query(tbl_type: ir.DataType, day_max=Q1_DAY) -> ir.Func:
     return fn
 
 
+# ----------------------------------------------------------------------------- high-card group-by
+def zipf_keys(n: int, ndistinct: int, s: float, rng) -> np.ndarray:
+    """n int64 keys: rank ~ Zipf(s) truncated to `ndistinct` ranks (inverse-CDF sampling), mapped
+    through a seeded permutation to distinct ids (an odd multiplier permutes the 2^40 space)."""
+    w = np.arange(1, ndistinct + 1, dtype=np.float64) ** (-s)
+    cdf = np.cumsum(w)
+    cdf /= cdf[-1]
+    ranks = np.searchsorted(cdf, rng.random(n), side="right")
+    np.minimum(ranks, ndistinct - 1, out=ranks)
+    mult = (int(rng.integers(1, 1 << 39)) << 1) | 1
+    ids = ((ranks.astype(np.uint64) * np.uint64(mult)) & np.uint64((1 << 40) - 1)).astype(np.int64)
+    return ids
+
+
+def hashgroup_table(n: int = 100_000_000, ndistinct: int = 10_000_000, s: float = 1.1, seed: int = 2) -> Table:
+    """n rows: key int64 (Zipf(s) over `ndistinct` ids, unsorted, flat), value f64 in [0,1000).
+    dim 2: the key is the first of two iterator columns, as a grouped vector."""
+    rng = np.random.default_rng(seed)
+    keys = zipf_keys(n, ndistinct, s, rng)
+    vals = rng.uniform(0.0, 1000.0, n)
+    return Table.from_arrays(2, {"key": keys, "value": vals}, name="zipf")
+
+
+def ree_sorted(t: Table) -> Table:
+    """The same rows stably sorted by key, key run-end encoded: the layout the reference's
+    grouped aggregation needs (a 2-d vector with a "+r" column 0, test_multidim.cpp)."""
+    from .table import ree_encode
+    order = np.argsort(t.columns[0].data, kind="stable")
+    keys = t.columns[0].data[order]
+    vals, ends = ree_encode(keys)
+    cols = {"key": vals}
+    for c in t.columns[1:]:
+        cols[c.name] = c.data[order]
+    return Table.from_arrays(2, cols, runend={"key": ends}, name=t.name + "_ree")
+
+
+def hashgroup_query(tbl_type: ir.DataType) -> ir.Func:
+    """Per key: SUM(value) f64 and COUNT i64 - an Op over the 2-d vector whose output reduces
+    each key's rows (the grouped form of test_multidim.cpp:9-29 and TPC-H Q18, tpch.h:687-715).
+    Over a run-end encoded key column it is the reference's segmented reduce; over a flat,
+    unsorted key column the GPU backend runs it as a hash group-by."""
+    vec = _sym("vec", tbl_type)
+    t = _sym("key", ir._i64_t)
+    red = _red(vec[t], lambda: _new([_f64(0), _i64(0)]),
+               lambda s, v: _new([_add(_get(s, 0), _get(v, 0)), _add(_get(s, 1), _i64(1))]))
+    red_sym = _sym("agg", red)
+    op = ir._op([t], ir._in(t, vec), [_get(red_sym, 0), _get(red_sym, 1)])
+    op_sym = _sym("op", op)
+    fn = _func("group_sum", op_sym, [vec])
+    fn.tbl[red_sym] = red
+    fn.tbl[op_sym] = op
+    return fn
+
+
 # ----------------------------------------------------------------------------- join + aggregate
 Q3_ATTR, Q3_DAY_LO, Q3_DAY_HI = 5, 0, 365
 
