@@ -161,7 +161,7 @@ struct rf_plan {
     long long* seg_woff = nullptr;
     long long* seg_tmp = nullptr;
     void* seg_part = nullptr;
-    size_t seg_runs_cap = 0, seg_part_cap = 0;
+    size_t seg_runs_cap = 0, seg_part_cap = 0, seg_tmp_cap = 0;
 };
 
 namespace {
@@ -394,6 +394,13 @@ extern "C" int rf_gpu_init(int device, rf_ctx** out)
     CUDA_TRY(nullptr, cudaFree(nullptr));
     if (!drv().ok) return RF_ERR_CUDA;
     CUDA_TRY(nullptr, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    // table buffers come from the device's stream-ordered pool; keep freed memory in the pool so
+    // per-run output tables do not go back to the driver
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        unsigned long long thr = ~0ULL;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
     CUDA_TRY(nullptr, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
     CUDA_TRY(nullptr, cudaMalloc((void**)&ctx->dev_err, sizeof(int)));
     CUDA_TRY(nullptr, cudaMemset(ctx->dev_err, 0, sizeof(int)));
@@ -483,14 +490,12 @@ int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src
     *active = nullptr;
     if (!src || bytes == 0) return RF_OK;
     if (!*buf || *cap < bytes) {
-        if (*buf) {
-            cudaStreamSynchronize(s);
-            cudaFree(*buf);
-        }
+        if (*buf) cudaFreeAsync(*buf, s);
         *buf = nullptr;
         *cap = 0;
         // 16 bytes of slack: vector loads may touch the tail of the last element's 16-byte line
-        if (cudaMalloc(buf, bytes + 16) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "cudaMalloc(%zu) failed", bytes);
+        if (cudaMallocAsync(buf, bytes + 16, s) != cudaSuccess)
+            return fail(ctx, RF_ERR_OOM, "cudaMallocAsync(%zu) failed", bytes);
         *cap = bytes;
     }
     CUDA_TRY(ctx, cudaMemcpyAsync(*buf, src, bytes, cudaMemcpyHostToDevice, s));
@@ -498,15 +503,20 @@ int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src
     return RF_OK;
 }
 
+// table buffers are pool allocations ordered on the context's stream
 void free_table_mem(rf_table* t)
 {
+    cudaStream_t s = t->ctx ? t->ctx->stream : nullptr;
     for (auto& c : t->cols) {
-        cudaFree(c.data_buf);
-        cudaFree(c.valid_buf);
-        cudaFree(c.re_buf);
+        if (c.data_buf) cudaFreeAsync(c.data_buf, s);
+        if (c.valid_buf) cudaFreeAsync(c.valid_buf, s);
+        if (c.re_buf) cudaFreeAsync(c.re_buf, s);
+        c.data_buf = c.valid_buf = c.re_buf = nullptr;
     }
-    cudaFree(t->ix_slots);
-    cudaFree(t->ix_special);
+    if (t->ix_slots) cudaFreeAsync(t->ix_slots, s);
+    if (t->ix_special) cudaFreeAsync(t->ix_special, s);
+    t->ix_slots = nullptr;
+    t->ix_special = nullptr;
 }
 
 }  // namespace
@@ -617,12 +627,12 @@ int build_index(rf_table* t, cudaStream_t s)
     if (!t->present[0]) return fail(ctx, RF_ERR_INVALID, "column 0 not on the device");
     unsigned long long cap = (unsigned long long)(2 * c0.nvals);  // load factor 0.5
     if (cap < 2) cap = 2;
-    cudaFree(t->ix_slots);
-    cudaFree(t->ix_special);
+    if (t->ix_slots) cudaFreeAsync(t->ix_slots, s);
+    if (t->ix_special) cudaFreeAsync(t->ix_special, s);
     t->ix_slots = nullptr;
     t->ix_special = nullptr;
-    if (cudaMalloc((void**)&t->ix_slots, cap * 16) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
-    if (cudaMalloc((void**)&t->ix_special, 8) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
+    if (cudaMallocAsync((void**)&t->ix_slots, cap * 16, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
+    if (cudaMallocAsync((void**)&t->ix_special, 8, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
     t->ix_cap = cap;
     int e = rf_k_index_build(c0.data, c0.valid, c0.nvals, t->ix_slots, cap, t->ix_special, ctx->dev_err, s);
     if (e) return fail(ctx, RF_ERR_CUDA, "index build launch failed: %s", cudaGetErrorString((cudaError_t)e));
@@ -649,8 +659,7 @@ extern "C" int rf_table_free(rf_table* t)
 {
     if (!t) return RF_OK;
     cudaSetDevice(t->ctx->device);
-    cudaStreamSynchronize(t->ctx->stream);
-    free_table_mem(t);
+    free_table_mem(t);  // stream-ordered: work already enqueued on the table still completes
     delete t;
     return RF_OK;
 }
@@ -1190,7 +1199,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         dc.type = pl.out_cols[c];
         dc.name = (c < (size_t)pl.out_dim ? "it" : "out") + std::to_string(c < (size_t)pl.out_dim ? c : c - pl.out_dim);
         size_t bytes = (size_t)std::max<long long>(cap, 1) * dc.type.size();
-        if (cudaMalloc(&dc.data_buf, bytes + 16) != cudaSuccess) {
+        if (cudaMallocAsync(&dc.data_buf, bytes + 16, s) != cudaSuccess) {
             free_table_mem(t.get());
             return fail(ctx, RF_ERR_OOM, "output column allocation (%zu bytes) failed", bytes);
         }
@@ -1199,7 +1208,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         hptrs[c] = dc.data_buf;
         if (pl.vectorize) {
             size_t vb = (size_t)((std::max<long long>(cap, 1) + 31) / 32) * 4;
-            if (cudaMalloc(&dc.valid_buf, vb + 16) != cudaSuccess) {
+            if (cudaMallocAsync(&dc.valid_buf, vb + 16, s) != cudaSuccess) {
                 free_table_mem(t.get());
                 return fail(ctx, RF_ERR_OOM, "output bitmap allocation failed");
             }
@@ -1231,9 +1240,8 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         nruns = vt->cols[0].nvals;
         long long nrows = vt->cols[0].logical;
         size_t wmax = (size_t)(nruns + (nrows + pl.seg_chunk - 1) / pl.seg_chunk + 2);
-        size_t cap1 = 0;
         if (!grow((void**)&p->seg_woff, &p->seg_runs_cap, (size_t)(nruns + 2) * 8, s) ||
-            !grow((void**)&p->seg_tmp, &cap1, (size_t)(nruns / 2048 + 4) * 8, s) ||
+            !grow((void**)&p->seg_tmp, &p->seg_tmp_cap, (size_t)(nruns / 2048 + 4) * 8, s) ||
             !grow(&p->seg_part, &p->seg_part_cap, wmax * pl.acc_bytes, s)) {
             free_table_mem(t.get());
             return fail(ctx, RF_ERR_OOM, "segmented-reduce buffers");
