@@ -272,7 +272,7 @@ def main():
     pargs = plan.args(*dts)
     n = len(dts)
     stream = eng.stream
-    out_check = plan.new_out()
+    out_check = None if plan.info.output_is_table else plan.new_out()
 
     table_out = bool(plan.info.output_is_table)
     out_rows = [0]

@@ -235,6 +235,7 @@ struct Space {
     std::vector<Expr> lbs, ubs;      // bound expressions (iter >= lb, iter <= ub)
     std::vector<Expr> filters;       // boolean symbols
     int n_vecs = 0;
+    std::vector<std::pair<int, Expr>> vecs;  // every iterated vector (Func input, In's vec)
 };
 
 class Lowerer {
@@ -760,9 +761,12 @@ private:
             auto f = input_index_.find(vec.get());
             if (f == input_index_.end()) throw LowerError("iteration over a non-input vector");
             sp.n_vecs++;
-            sp.has_vec = true;
-            sp.vec_input = f->second;
-            sp.vec_node = in->vec;
+            sp.vecs.push_back({f->second, in->vec});
+            if (!sp.has_vec) {
+                sp.has_vec = true;
+                sp.vec_input = f->second;
+                sp.vec_node = in->vec;
+            }
             return;
         }
         throw LowerError("predicate node not lowered");
@@ -777,7 +781,6 @@ private:
         for (auto& s : fn_->inputs)
             if (s->type.is_val()) vars.insert(s.get());
         space_of(op.pred, sp.iter, vars, sp);
-        if (sp.n_vecs > 1) throw LowerError("merge co-iteration is lowered by the join template");
         if (!sp.has_vec && sp.lbs.empty()) throw LowerError("unbounded iteration space (no lower bound)");
         if (!sp.has_vec && sp.ubs.empty()) throw LowerError("unbounded iteration space (no upper bound)");
         return sp;
@@ -1281,6 +1284,7 @@ private:
         Drive d;
         if (red.vec->kind == NodeKind::OP) {
             d.sp = op_space(*as<Op>(red.vec));
+            if (d.sp.n_vecs > 1) throw LowerError("a Reduce over a merge co-iteration is not lowered");
             if (d.sp.has_vec) {
                 d.input = d.sp.vec_input;
                 d.slot = plan_.table_slot[d.input];
@@ -2058,6 +2062,122 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
         if (d.sp.iter->type.btype != INT64) throw LowerError("hash group-by keys must be int64");
     }
 
+    // Merge co-iteration (InterSpace, iter_space.cpp:217-250,318-364): the loop walks the
+    // sorted iterator columns of every vector and emits a row where all of them hold the same
+    // value.  Here each row r of the first vector is an element: its partner in vector k is found
+    // by binary search - the row at (first row of the key in k) + (rank of r among equal keys in
+    // the first vector), which is how the two-pointer walk pairs duplicates.  Starts come from
+    // Locate(max(lbs, first values)) as the merge's lower bound does; requires sorted columns.
+    void lower_merge_join(const Op& op, const Drive& d)
+    {
+        plan_.kind = PlanKind::MERGE_JOIN;
+        const Space& sp = d.sp;
+        const int T = plan_.threads;
+        if (sp.vecs.size() > 4) throw LowerError("merge co-iteration of more than 4 vectors");
+        if (!(sp.iter->type.is_int() || sp.iter->type.is_idx())) throw LowerError("merge join over a non-integer iterator");
+        std::string Ty = ctype(sp.iter->type);
+        std::vector<int> slots;
+        for (auto& v : sp.vecs) {
+            slots.push_back(plan_.table_slot[v.first]);
+            plan_.needs_index[v.first] = 1;
+            if (fn_->inputs[v.first]->type.dim != 1) throw LowerError("merge join over a 2-d vector");
+        }
+        std::ostringstream o;
+        o << "// generated by the reffine_gb300 lowering pass: " << fn_->name << " (merge co-iteration)\n";
+        o << "#include \"rf_device.cuh\"\n\n";
+        // range kernel: L, U, per-vector start rows
+        {
+            Emitter E(*this);
+            bind_inputs(E);
+            std::string first, last;
+            for (size_t k = 0; k < slots.size(); k++) {
+                std::string c = "P.t[" + std::to_string(slots[k]) + "].col[0]";
+                std::string f = "rf_rd<" + Ty + ">(" + c + ", 0)";
+                std::string l = "rf_rd<" + Ty + ">(" + c + ", " + c + ".len - 1)";
+                first = first.empty() ? f : "rf_max<" + Ty + ">(" + f + ", " + first + ")";
+                last = last.empty() ? l : "rf_min<" + Ty + ">(" + l + ", " + last + ")";
+            }
+            std::string L = bound_expr(E, sp.lbs, first, true, sp.iter->type);
+            std::string U = sp.ubs.empty() ? last : bound_expr(E, sp.ubs, last, false, sp.iter->type);
+            o << "extern \"C\" __global__ void rf_range(const __grid_constant__ RfParams P)\n{\n";
+            o << "    if (threadIdx.x != 0 || blockIdx.x != 0) return;\n";
+            for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+            o << "    const " << Ty << " L = " << L << ";\n    const " << Ty << " U = " << U << ";\n";
+            o << "    bool empty = false;\n";
+            for (size_t k = 0; k < slots.size(); k++) {
+                std::string t = "P.t[" + std::to_string(slots[k]) + "]";
+                o << "    long long s" << k << " = " << t << ".col[0].len > 0 ? rf_locate(" << t << ".ix, (long long)L) : -1;\n";
+                o << "    if (" << t << ".col[0].len == 0) empty = true; else if (s" << k << " < 0) { rf_set_err(P, RF_DEVERR_RANGE); empty = true; }\n";
+            }
+            o << "    P.range[0] = empty ? 0 : s0;\n    P.range[1] = empty ? 0 : P.t[" << slots[0] << "].col[0].len;\n";
+            o << "    P.range[2] = (long long)L;\n    P.range[3] = (long long)U;\n";
+            for (size_t k = 1; k < slots.size(); k++) o << "    P.range[" << 3 + k << "] = s" << k << " < 0 ? 0 : s" << k << ";\n";
+            o << "}\n\n";
+            plan_.kernels.push_back({"rf_range", 32, 0, KernelSpec::RANGE});
+            plan_.device_range = true;
+        }
+        o << "RF_DEV long long rf_lower_bound(const RfCol& c, long long lo, long long hi, " << Ty << " key)\n{\n";
+        o << "    while (lo < hi) { long long mid = (lo + hi) >> 1; if (rf_ld<" << Ty << ">(c.data, mid) < key) lo = mid + 1; else hi = mid; }\n";
+        o << "    return lo;\n}\n\n";
+        auto body_of = [&](Emitter& E, std::ostringstream& b) -> std::string {
+            std::string a = "P.t[" + std::to_string(slots[0]) + "].col[0]";
+            b << "    const " << Ty << " it = rf_ld<" << Ty << ">(" << a << ".data, r);\n";
+            b << "    const long long rank = r - rf_lower_bound(" << a << ", P.range[0], r, it);\n";
+            b << "    bool mt = rf_valid(" << a << ".valid, r) && it >= (" << Ty << ")P.range[2] && it <= (" << Ty << ")P.range[3];\n";
+            E.vec_iter_idx[{sp.vecs[0].second.get(), sp.iter.get()}] = "r";
+            for (size_t k = 1; k < slots.size(); k++) {
+                std::string c = "P.t[" + std::to_string(slots[k]) + "].col[0]";
+                std::string j = "j" + std::to_string(k);
+                b << "    const long long " << j << " = rf_lower_bound(" << c << ", P.range[" << 3 + k << "], " << c
+                  << ".len, it) + rank;\n";
+                b << "    mt = mt && " << j << " < " << c << ".len && rf_ld<" << Ty << ">(" << c << ".data, " << j
+                  << ") == it && rf_valid(" << c << ".valid, " << j << ");\n";
+                E.vec_iter_idx[{sp.vecs[k].second.get(), sp.iter.get()}] = j;
+            }
+            E.bind(op.iters[0], E.scalar("it", sp.iter->type));
+            std::string cond = "mt";
+            for (auto& f : sp.filters) cond += " && (" + E.ev(f).c + ")";
+            return cond;
+        };
+        {
+            Emitter E(*this);
+            bind_inputs(E);
+            std::ostringstream b;
+            std::string cond = body_of(E, b);
+            o << "RF_DEV bool rf_cond(const RfParams& P, long long r)\n{\n" << b.str();
+            for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+            o << "    return " << cond << ";\n}\n\n";
+        }
+        {
+            Emitter E(*this);
+            bind_inputs(E);
+            E.in_bounds_rows = false;
+            std::ostringstream b;
+            body_of(E, b);
+            std::ostringstream w;
+            size_t c = 0;
+            w << "    ((" << Ty << "*)((void* const*)P.aux0)[" << c++ << "])[o] = it;\n";
+            for (auto& x : op.outputs) {
+                w << "    ((" << ctype(x->type) << "*)((void* const*)P.aux0)[" << c << "])[o] = (" << ctype(x->type) << ")("
+                  << E.ev(x).c << ");\n";
+                c++;
+            }
+            o << "RF_DEV void rf_emit(const RfParams& P, long long r, long long o)\n{\n" << b.str();
+            for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+            o << w.str() << "}\n\n";
+        }
+        o << "#define RF_MATERIALIZE 1\n#include \"rf_templates.cuh\"\n";
+        o << "RF_MATERIALIZE_KERNELS(" << T << ", " << plan_.out_cols.size() << ")\n";
+        if (vectorize_) {
+            plan_.kernels.push_back({"rf_write_all", T, 0, KernelSpec::FINAL});
+        } else {
+            plan_.kernels.push_back({"rf_count", T, 0, KernelSpec::COUNT});
+            plan_.kernels.push_back({"rf_scan", 1024, 0, KernelSpec::SCAN});
+            plan_.kernels.push_back({"rf_scatter", T, 0, KernelSpec::SCATTER});
+        }
+        plan_.source = o.str();
+    }
+
     void lower_op(const Expr& opx)
     {
         const Op& op = *as<Op>(opx);
@@ -2072,6 +2192,10 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
         Drive d;
         d.sp = op_space(op);
         drive_rows(d);
+        if (d.sp.n_vecs > 1) {
+            lower_merge_join(op, d);
+            return;
+        }
         plan_.kind = PlanKind::MATERIALIZE;
         const int T = plan_.threads;
         std::ostringstream src;

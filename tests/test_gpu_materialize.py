@@ -116,3 +116,40 @@ def plan_run_table(eng, plan, *inputs):
         return dt.export()
     finally:
         dt.free()
+
+
+def test_join_op_merge_coiteration(eng):
+    # JoinOpTest (test_join.cpp:39-87): three tables generated by the gen_table query itself
+    g = eng.compile(rq.gen_table_op())
+    bounds = [(0, 10), (5, 15), (7, 12)]
+    ts = []
+    for lo, hi in bounds:
+        out = plan_run_table(eng, g, lo, hi)
+        ts.append(Table.from_arrays(1, {"t": out["cols"][0], "v": out["cols"][1]}))
+    fn = rq.join_op(*ts)
+    plan = eng.compile(fn)
+    assert plan.kind == 6
+    out = plan_run_table(eng, plan, *ts)
+    lb, ub = max(b[0] for b in bounds), min(b[1] for b in bounds)
+    assert out["len"] == ub - lb
+    np.testing.assert_array_equal(out["cols"][0], np.arange(lb, ub))
+    np.testing.assert_array_equal(out["cols"][1], 3 * np.arange(lb, ub))
+    assert_table_same(out, loopgen.Query(fn)(*ts))
+
+
+def test_merge_join_sorted_with_gaps_and_duplicates(eng):
+    rng = np.random.default_rng(12)
+    a = np.sort(rng.integers(0, 50_000, 100_000))
+    b = np.sort(rng.integers(0, 50_000, 60_000))
+    a[0] = b[0] = 0
+    ta = Table.from_arrays(1, {"t": a.astype(np.int64), "v": rng.integers(0, 1000, len(a))})
+    tb = Table.from_arrays(1, {"t": b.astype(np.int64), "v": rng.integers(0, 1000, len(b))})
+    tt = _sym("t", _i64_t)
+    av, bv = _sym("av", ta.get_data_type()), _sym("bv", tb.get_data_type())
+    x, y = av[tt][0], bv[tt][0]
+    op = _op([tt], _in(tt, av) & _in(tt, bv), [_add(x, y)])
+    os_ = _sym("op", op)
+    fn = _func("mj", os_, [av, bv])
+    fn.tbl[os_] = op
+    out = plan_run_table(eng, eng.compile(fn), ta, tb)
+    assert_table_same(out, loopgen.Query(fn)(ta, tb))
