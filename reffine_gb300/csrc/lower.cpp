@@ -1806,12 +1806,15 @@ private:
     // unsorted.  The groups are the distinct valid keys - the runs the reference would see after
     // sorting and run-end encoding - so each output row is the same; rows come out in slot order.
     //   rf_hg_init  fills the table: keys RF_EMPTY_KEY, accumulators at their identity
-    //   rf_hg_agg   one pass over the rows: a per-block shared-memory table pre-aggregates the
-    //               frequent keys, the rest go to the global open-addressing table (load 0.5)
+    //   rf_hg_agg   one pass over the rows.  A per-block shared-memory table takes the keys a
+    //               block meets first - under a skewed distribution the frequent ones - and
+    //               absorbs their updates with shared-memory atomics; a key found neither there
+    //               nor in a free shared slot goes to the global open-addressing table (load 0.5)
     //   rf_cond / rf_emit   the materialisation template over the slots
-    // Device layout: keys (long long*)P.aux4 [C + 1] (slot C: the key RF_EMPTY_KEY itself, used
-    // flag in its key word), accumulators (unsigned long long*)P.aux5 [L][C + 1], rows P.aux_n0,
-    // capacity C = P.aux_n1.
+    // Global slots are array-of-structs, {key, accumulators...} padded to RF_HG_SW 8-byte words
+    // (one 32-byte sector for up to three accumulators), so a row touches one sector.
+    // Device layout: slots (unsigned long long*)P.aux4 [C + 1][RF_HG_SW] (slot C: the key
+    // RF_EMPTY_KEY itself, a used flag in its key word), rows P.aux_n0, capacity C = P.aux_n1.
     void lower_hash_group(const Op& op, const Drive& d, const Reduce& red)
     {
         plan_.kind = PlanKind::HASH_GROUP;
@@ -1827,7 +1830,11 @@ private:
         std::string c0 = "P.t[" + sl + "].col[0]";
         std::ostringstream o;
         o << "// generated by the reffine_gb300 lowering pass: " << fn_->name << " (hash group-by)\n";
-        o << "#include \"rf_device.cuh\"\n\n#define RF_HG_L " << std::max(L, 1) << "\n#define RF_HG_S " << S << "\n\n";
+        const int SW = L + 1 <= 4 ? 4 : (L + 1 <= 8 ? 8 : 16);
+        if (L + 1 > 16) throw LowerError("hash group-by with more than 15 aggregates");
+        o << "#include \"rf_device.cuh\"\n\n#define RF_HG_L " << std::max(L, 1) << "\n#define RF_HG_S " << S
+          << "\n#define RF_HG_SW " << SW << "\n\n";
+        plan_.acc_bytes = (size_t)SW * 8;
         auto kind_of = [&](const Leaf& lf) -> std::string {
             bool f = lf.type.is_float() && !lf.count;
             switch (lf.op) {
@@ -1902,17 +1909,21 @@ private:
         o << R"(// slot of `key` in the global table (claimed if new); C + 1 slots, slot C is the empty key's
 RF_DEV long long rf_hg_slot(const RfParams& P, long long key)
 {
-    long long* keys = (long long*)P.aux4;
+    unsigned long long* tab = (unsigned long long*)P.aux4;
     const unsigned long long C = (unsigned long long)P.aux_n1;
     if (key == RF_EMPTY_KEY) {
-        if (keys[C] == 0) atomicExch((unsigned long long*)(keys + C), 1ULL);
+        if (tab[C * RF_HG_SW] == 0) atomicExch(tab + C * RF_HG_SW, 1ULL);
         return (long long)C;
     }
     unsigned long long h = rf_home(key, C);
     for (unsigned long long n = 0; n < C; ++n) {
-        unsigned long long old = atomicCAS((unsigned long long*)(keys + h), (unsigned long long)RF_EMPTY_KEY,
-                                           (unsigned long long)key);
-        if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) return (long long)h;
+        unsigned long long* kp = tab + h * RF_HG_SW;
+        unsigned long long cur = __ldcg(kp);
+        if (cur == (unsigned long long)key) return (long long)h;
+        if (cur == (unsigned long long)RF_EMPTY_KEY) {
+            unsigned long long old = atomicCAS(kp, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)key);
+            if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) return (long long)h;
+        }
         if (++h == C) h = 0;
     }
     rf_set_err(P, RF_DEVERR_OVERFLOW);
@@ -1921,12 +1932,12 @@ RF_DEV long long rf_hg_slot(const RfParams& P, long long key)
 
 extern "C" __global__ void __launch_bounds__(256) rf_hg_init(const __grid_constant__ RfParams P)
 {
-    long long* keys = (long long*)P.aux4;
-    unsigned long long* acc = (unsigned long long*)P.aux5;
+    unsigned long long* tab = (unsigned long long*)P.aux4;
     const long long C = P.aux_n1;
     for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s <= C; s += (long long)gridDim.x * blockDim.x) {
-        keys[s] = s < C ? RF_EMPTY_KEY : 0;
-        for (int l = 0; l < RF_HG_L; l++) acc[(long long)l * (C + 1) + s] = rf_hg_identity(P, l);
+        unsigned long long* sl = tab + s * RF_HG_SW;
+        sl[0] = s < C ? (unsigned long long)RF_EMPTY_KEY : 0ULL;
+        for (int l = 0; l < RF_HG_L; l++) sl[1 + l] = rf_hg_identity(P, l);
     }
 }
 
@@ -1936,26 +1947,32 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
     __shared__ unsigned long long sv[RF_HG_L * RF_HG_S];
     for (int i = threadIdx.x; i < RF_HG_S; i += blockDim.x) {
         sk[i] = RF_EMPTY_KEY;
-        for (int l = 0; l < RF_HG_L; l++) sv[l * RF_HG_S + i] = rf_hg_identity(P, l);
+        for (int l = 0; l < RF_HG_L; l++) sv[i * RF_HG_L + l] = rf_hg_identity(P, l);
     }
     __syncthreads();
-    unsigned long long* acc = (unsigned long long*)P.aux5;
-    const long long C = P.aux_n1, n = P.aux_n0;
+    unsigned long long* tab = (unsigned long long*)P.aux4;
+    const long long n = P.aux_n0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
 )";
         o << "        if (!rf_valid(" << c0 << ".valid, r)) continue;  // a null key is no group\n";
         o << "        const long long key = rf_ld<int64_t>(" << c0 << ".data, r);\n";
         o << R"(        unsigned long long* A = nullptr;
-        long long st = 0;
         if (key != RF_EMPTY_KEY) {
+            // read-only probe first; claim a free slot only when the probe reaches one
             unsigned h = (unsigned)rf_home(key, RF_HG_S);
             for (int p = 0; p < 8; p++) {
-                unsigned long long old = atomicCAS((unsigned long long*)&sk[h], (unsigned long long)RF_EMPTY_KEY,
-                                                   (unsigned long long)key);
-                if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) {
-                    A = sv + h;
-                    st = RF_HG_S;
+                long long cur = ((volatile long long*)sk)[h];
+                if (cur == key) {
+                    A = sv + h * RF_HG_L;
                     break;
+                }
+                if (cur == RF_EMPTY_KEY) {
+                    unsigned long long old = atomicCAS((unsigned long long*)&sk[h], (unsigned long long)RF_EMPTY_KEY,
+                                                       (unsigned long long)key);
+                    if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) {
+                        A = sv + h * RF_HG_L;
+                        break;
+                    }
                 }
                 if (++h == RF_HG_S) h = 0;
             }
@@ -1963,34 +1980,32 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
         if (!A) {
             long long g = rf_hg_slot(P, key);
             if (g < 0) continue;
-            A = acc + g;
-            st = C + 1;
+            A = tab + g * RF_HG_SW + 1;
         }
-        rf_hg_apply(P, r, A, st);
+        rf_hg_apply(P, r, A, 1);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < RF_HG_S; i += blockDim.x) {
         if (sk[i] == RF_EMPTY_KEY) continue;
         long long g = rf_hg_slot(P, sk[i]);
-        if (g >= 0) rf_hg_merge(P, acc + g, C + 1, sv + i, RF_HG_S);
+        if (g >= 0) rf_hg_merge(P, tab + g * RF_HG_SW + 1, 1, sv + i * RF_HG_L, 1);
     }
 }
 
 )";
         // element functions over the slots
         auto elem = [&](Emitter& E, std::ostringstream& body) {
-            body << "    const long long* keys = (const long long*)P.aux4;\n";
-            body << "    const unsigned long long* acc = (const unsigned long long*)P.aux5;\n";
+            body << "    const unsigned long long* sl = (const unsigned long long*)P.aux4 + r * RF_HG_SW;\n";
             body << "    const long long C = P.aux_n1;\n";
-            body << "    const bool used = r < C ? keys[r] != RF_EMPTY_KEY : keys[C] != 0;\n";
-            body << "    const int64_t it = r < C ? keys[r] : RF_EMPTY_KEY;\n";
+            body << "    const bool used = r < C ? (long long)sl[0] != RF_EMPTY_KEY : sl[0] != 0;\n";
+            body << "    const int64_t it = r < C ? (long long)sl[0] : RF_EMPTY_KEY;\n";
             E.bind(op.iters[0], E.scalar("it", d.sp.iter->type));
             std::map<std::vector<size_t>, std::string> finals;
             for (size_t i = 0, k = 0; i < leaves.size(); i++) {
                 auto& lf = leaves[i];
                 std::string tot = "0";
                 if (lf.op != AggOp::NONE) {
-                    std::string raw = "acc[" + std::to_string(k) + " * (C + 1) + r]";
+                    std::string raw = "sl[" + std::to_string(k + 1) + "]";
                     tot = (lf.type.is_float() && !lf.count) ? "rf_u2f(" + raw + ")" : "(long long)(" + raw + ")";
                     k++;
                 }
@@ -2055,7 +2070,6 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
         plan_.kernels.push_back({"rf_count", T, 0, KernelSpec::COUNT});
         plan_.kernels.push_back({"rf_scan", 1024, 0, KernelSpec::SCAN});
         plan_.kernels.push_back({"rf_scatter", T, 0, KernelSpec::SCATTER});
-        plan_.acc_bytes = (size_t)std::max(L, 1) * 8;
         plan_.aggs = L;
         plan_.device_range = false;
         plan_.source = o.str();

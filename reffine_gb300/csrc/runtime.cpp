@@ -1172,12 +1172,10 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         if ((rc = ndv_estimate(vt, 0, s, &ndv))) return rc;
         hg_cap = std::max<long long>(1024, (long long)(2.2 * (double)ndv));
         if (p->hg_retry_cap > hg_cap) hg_cap = p->hg_retry_cap;
-        size_t L = std::max<size_t>(1, pl.acc_bytes / 8);
-        if (!grow(&p->hg_keys, &p->hg_keys_cap, (size_t)(hg_cap + 1) * 8, s) ||
-            !grow(&p->hg_acc, &p->hg_acc_cap, (size_t)(hg_cap + 1) * 8 * L, s))
+        // slots of pl.acc_bytes bytes: {key, accumulators} (array of structs)
+        if (!grow(&p->hg_keys, &p->hg_keys_cap, (size_t)(hg_cap + 1) * pl.acc_bytes, s))
             return fail(ctx, RF_ERR_OOM, "hash table allocation (%lld slots)", hg_cap);
         P.aux4 = p->hg_keys;
-        P.aux5 = p->hg_acc;
         P.aux_n0 = vt->cols[0].logical;
         P.aux_n1 = hg_cap;
         lo = 0;
