@@ -44,9 +44,12 @@ __global__ void index_build_kernel(const long long* __restrict__ keys, const uns
         // bounded: at most `cap` probes (the table is half empty, so a few in practice)
         for (unsigned long long p = 0; p < cap; ++p) {
             unsigned long long* kp = reinterpret_cast<unsigned long long*>(slots + 2 * h);
-            unsigned long long old = atomicCAS(kp, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)k);
+            // read first: duplicated keys find their slot without an atomic on the key word
+            unsigned long long old = __ldcg(kp);
+            if (old == (unsigned long long)RF_EMPTY_KEY)
+                old = atomicCAS(kp, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)k);
             if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)k) {
-                atomicMin(slots + 2 * h + 1, i);
+                if (__ldcg(slots + 2 * h + 1) > i) atomicMin(slots + 2 * h + 1, i);
                 done = true;
                 break;
             }

@@ -1825,7 +1825,7 @@ private:
         for (size_t i = 0; i < leaves.size(); i++)
             if (leaves[i].op != AggOp::NONE) act.push_back((int)i);
         const int L = (int)act.size();
-        const int S = std::max(256, std::min(2048, (int)(96 * 1024 / (8 * (L + 1)))));
+        const int S = std::max(256, std::min(1024, (int)(24 * 1024 / (8 * (L + 1)))));
         std::string sl = std::to_string(d.slot);
         std::string c0 = "P.t[" + sl + "].col[0]";
         std::ostringstream o;
@@ -1952,11 +1952,22 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
     __syncthreads();
     unsigned long long* tab = (unsigned long long*)P.aux4;
     const long long n = P.aux_n0;
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // four rows per thread per step: their key loads are issued together
+    for (long long r0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; r0 < n; r0 += 4 * stride) {
+        long long kk[4];
+        bool ok[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            long long r = r0 + j * stride;
 )";
-        o << "        if (!rf_valid(" << c0 << ".valid, r)) continue;  // a null key is no group\n";
-        o << "        const long long key = rf_ld<int64_t>(" << c0 << ".data, r);\n";
-        o << R"(        unsigned long long* A = nullptr;
+        o << "            ok[j] = r < n && rf_valid(" << c0 << ".valid, r);  // a null key is no group\n";
+        o << "            kk[j] = r < n ? rf_ld<int64_t>(" << c0 << ".data, r) : 0;\n        }\n";
+        o << R"(#pragma unroll 1
+        for (int j = 0; j < 4; j++) {
+        if (!ok[j]) continue;
+        const long long r = r0 + j * stride, key = kk[j];
+        unsigned long long* A = nullptr;
         if (key != RF_EMPTY_KEY) {
             // read-only probe first; claim a free slot only when the probe reaches one
             unsigned h = (unsigned)rf_home(key, RF_HG_S);
@@ -1983,6 +1994,7 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
             A = tab + g * RF_HG_SW + 1;
         }
         rf_hg_apply(P, r, A, 1);
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < RF_HG_S; i += blockDim.x) {
@@ -2072,6 +2084,7 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
         plan_.kernels.push_back({"rf_scatter", T, 0, KernelSpec::SCATTER});
         plan_.aggs = L;
         plan_.device_range = false;
+        std::fill(plan_.needs_index.begin(), plan_.needs_index.end(), 0);
         plan_.source = o.str();
         if (d.sp.iter->type.btype != INT64) throw LowerError("hash group-by keys must be int64");
     }

@@ -1264,7 +1264,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         if (k.role == rfg::KernelSpec::SEGCOUNT || k.role == rfg::KernelSpec::SEGREDUCE ||
             k.role == rfg::KernelSpec::INIT)
             grid = ctx->sm_count * 8;
-        if (pl.kind == rfg::PlanKind::HASH_GROUP && k.role == rfg::KernelSpec::MAIN) grid = ctx->sm_count * 2;
+        if (pl.kind == rfg::PlanKind::HASH_GROUP && k.role == rfg::KernelSpec::MAIN) grid = p->max_units;
         if (k.role == rfg::KernelSpec::RANGE || k.role == rfg::KernelSpec::SCAN) grid = 1;
         if (k.role == rfg::KernelSpec::STOP)
             grid = (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8);
