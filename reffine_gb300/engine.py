@@ -236,6 +236,7 @@ class Plan:
                 arr[i].kind, arr[i].f64 = _capi.RF_ARG_F64, float(v)
             else:
                 arr[i].kind, arr[i].i64 = _capi.RF_ARG_I64, int(v)
+        arr._inputs = inputs  # the device tables must outlive the argument array
         return arr
 
     def run(self, *inputs):
