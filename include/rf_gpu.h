@@ -137,6 +137,21 @@ int rf_plan_run(rf_plan* plan, const rf_arg* args, int32_t n_args, void* out, vo
 /* Enqueues a run without waiting.  Value outputs land in device memory `dev_out`
  * (output_size bytes); table outputs are not allowed here. */
 int rf_plan_launch(rf_plan* plan, const rf_arg* args, int32_t n_args, void* dev_out, void* stream);
+/* rf_plan_run for callers that cannot allocate device memory while running queries - a host
+ * with a fixed device-memory budget decided at start-up, or a latency-critical loop where a
+ * cudaMalloc/cudaFree would synchronise the device.  It allocates nothing: the plan's partial
+ * results, completion counter, loop bounds and result live in one fixed array of 1 MiB that the
+ * library holds in device memory (on every device that loads it, until the process exits);
+ * runs needing more are rejected with RF_ERR_INVALID and a message saying so (the environment
+ * variable RF_NOALLOC_LIMIT, in bytes, lowers that limit; it cannot raise it).  Value-output
+ * (Reduce) plans only, and every table a plan probes must already have its index
+ * (rf_table_build_index), since building one allocates.  `host_out` receives the result, as in
+ * rf_plan_run; the call waits for it.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current.  All calls share the array, which
+ * keeps the last call's contents: calls that overlap on the GPU (other threads or streams)
+ * race and must be serialised by the caller.
+ * No counterpart in the reference (its generated code runs on the host). */
+int rf_plan_run_noalloc(rf_plan* plan, const rf_arg* args, int32_t n_args, void* host_out, void* stream);
 /* A host function with the signature of the reference's generated query function:
  *   void fn(OutT* output_addr, ArrowTable* in0, ..., int64/double scalars ...)
  * Each call copies its host tables' referenced columns to the device, runs the plan and writes

@@ -61,6 +61,7 @@ SIGNATURES = {
     "rf_plan_source": (ctypes.c_char_p, [P]),
     "rf_plan_run": (I, [P, ctypes.POINTER(RfArg), I32, P, P]),
     "rf_plan_launch": (I, [P, ctypes.POINTER(RfArg), I32, P, P]),
+    "rf_plan_run_noalloc": (I, [P, ctypes.POINTER(RfArg), I32, P, P]),
     "rf_plan_thunk": (I, [P, PP]),
     "rf_batch_create": (I, [P, I32, PP]),
     "rf_batch_free": (I, [P]),

@@ -207,3 +207,32 @@ extern "C" int rf_k_hll(const void* keys, const unsigned short* valid, long long
     hll_kernel<<<blocks, 512, 0, stream>>>(static_cast<const long long*>(keys), valid, n, regs);
     return (int)cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------------------
+// Fixed scratch for rf_plan_run_noalloc: callers that may not allocate device memory on the
+// query path run value-output plans with their partials, completion counter, loop bounds and
+// result placed here.  The array exists on every device that loads this library, for the life
+// of the process.  In host code `rf_noalloc_scratch` only names the variable; its device
+// address comes from cudaGetSymbolAddress, looked up once per device with that device current.
+// ---------------------------------------------------------------------------------------
+#include <mutex>
+
+#define RF_NOALLOC_SCRATCH_BYTES (1u << 20)
+static __device__ __align__(256) unsigned char rf_noalloc_scratch[RF_NOALLOC_SCRATCH_BYTES];
+
+extern "C" int rf_k_noalloc_scratch(int device, void** ptr, size_t* bytes)
+{
+    static std::mutex mu;
+    static void* addr[256] = {};
+    if (device < 0 || device >= 256) return (int)cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(mu);
+    if (!addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, rf_noalloc_scratch);
+        if (e != cudaSuccess) return (int)e;
+        addr[device] = p;
+    }
+    *ptr = addr[device];
+    *bytes = RF_NOALLOC_SCRATCH_BYTES;
+    return 0;
+}

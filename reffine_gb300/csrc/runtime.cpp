@@ -978,7 +978,8 @@ extern "C" int rf_plan_info(rf_plan* p, rf_plan_info_t* info)
 
 namespace rfrt {
 
-int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long long& lo, long long& hi)
+int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long long& lo, long long& hi,
+                bool may_allocate)
 {
     rf_ctx* ctx = p->ctx;
     const rfg::Plan& pl = p->plan;
@@ -1010,6 +1011,8 @@ int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long lo
                 if (!t->present[c]) return fail(ctx, RF_ERR_INVALID, "input %d: column %d is not on the device", i, c);
             if (pl.needs_index[i]) {
                 if (!t->has_index) {
+                    if (!may_allocate)
+                        return fail(ctx, RF_ERR_INVALID, "input %d needs its index: call rf_table_build_index first", i);
                     int rc = build_index(t, ctx->stream);
                     if (rc) return rc;
                 }
@@ -1060,7 +1063,7 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
     rf_ctx* ctx = p->ctx;
     RfParams P;
     long long lo, hi;
-    int rc = fill_params(p, args, n_args, P, lo, hi);
+    int rc = fill_params(p, args, n_args, P, lo, hi, true);
     if (rc) return rc;
     const rfg::Plan& pl = p->plan;
     long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
@@ -1161,7 +1164,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     const rfg::Plan& pl = p->plan;
     RfParams P;
     long long lo, hi;
-    int rc = fill_params(p, args, n_args, P, lo, hi);
+    int rc = fill_params(p, args, n_args, P, lo, hi, true);
     if (rc) return rc;
     long long hg_cap = 0;
     if (pl.kind == rfg::PlanKind::HASH_GROUP) {
@@ -1308,6 +1311,59 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
 }
 
 }  // namespace
+
+extern "C" int rf_plan_run_noalloc(rf_plan* p, const rf_arg* args, int32_t n_args, void* host_out, void* stream)
+{
+    if (!p) return RF_ERR_INVALID;
+    rf_ctx* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    const rfg::Plan& pl = p->plan;
+    if (pl.out_is_table || (pl.kind != rfg::PlanKind::SCAN_REDUCE && pl.kind != rfg::PlanKind::GROUP_REDUCE))
+        return fail(ctx, RF_ERR_UNSUPPORTED, "rf_plan_run_noalloc runs Reduce (value-output) plans only");
+    if (!host_out) return fail(ctx, RF_ERR_INVALID, "host_out is required");
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    void* base = nullptr;
+    size_t cap = 0;
+    int e = rf_k_noalloc_scratch(ctx->device, &base, &cap);
+    if (e) return fail(ctx, RF_ERR_CUDA, "scratch address lookup failed: %s", cudaGetErrorString((cudaError_t)e));
+    // RF_NOALLOC_LIMIT (bytes) can only lower the usable part of the array
+    if (const char* lim = getenv("RF_NOALLOC_LIMIT")) {
+        long long v = atoll(lim);
+        if (v > 0 && (size_t)v < cap) cap = (size_t)v;
+    }
+    RfParams P;
+    long long lo, hi;
+    int rc = fill_params(p, args, n_args, P, lo, hi, false);
+    if (rc) return rc;
+    long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
+    int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+    // layout: [counter 256][loop bounds 256][result, 256-aligned][partials: units x acc_bytes]
+    size_t out_bytes = (pl.out_size + 255) / 256 * 256;
+    size_t need = 512 + out_bytes + (size_t)units * pl.acc_bytes;
+    if (need > cap)
+        return fail(ctx, RF_ERR_INVALID,
+                    "rf_plan_run_noalloc: this run needs %zu bytes of scratch, the fixed array holds %zu "
+                    "(use rf_plan_run)", need, cap);
+    unsigned char* b = (unsigned char*)base;
+    P.counter = (unsigned int*)b;
+    P.range = pl.device_range ? (long long*)(b + 256) : nullptr;
+    P.out = b + 512;
+    P.partials = b + 512 + out_bytes;
+    P.nunits = units;
+    // the last-unit-done merge counts arrivals from zero
+    CUDA_TRY(ctx, cudaMemsetAsync(P.counter, 0, sizeof(unsigned int), s));
+    for (size_t i = 0; i < pl.kernels.size(); i++) {
+        const auto& k = pl.kernels[i];
+        int grid = k.role == rfg::KernelSpec::RANGE ? 1
+                   : k.role == rfg::KernelSpec::STOP
+                       ? (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8)
+                       : units;
+        if ((rc = launch(ctx, p->fns[i], grid, k.threads, k.smem, s, &P))) return rc;
+    }
+    CUDA_TRY(ctx, cudaMemcpyAsync(host_out, P.out, pl.out_size, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return check_device_error(ctx);
+}
 
 extern "C" int rf_plan_run(rf_plan* p, const rf_arg* args, int32_t n_args, void* out, void* stream)
 {
