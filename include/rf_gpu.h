@@ -168,6 +168,9 @@ int rf_batch_add(rf_batch* b, rf_plan* plan, const rf_arg* args, int32_t n_args,
  * replayed when the same set of plans recurs). */
 int rf_batch_launch(rf_batch* b, void* stream);
 int rf_batch_wait(rf_batch* b);
+/* Non-blocking: *done = 1 once the launched batch has finished (its results are then copied as
+ * by rf_batch_wait), 0 while it runs. */
+int rf_batch_poll(rf_batch* b, int32_t* done);
 int rf_batch_reset(rf_batch* b);
 
 #ifdef __cplusplus

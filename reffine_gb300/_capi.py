@@ -69,6 +69,7 @@ SIGNATURES = {
     "rf_batch_launch": (I, [P, P]),
     "rf_batch_wait": (I, [P]),
     "rf_batch_reset": (I, [P]),
+    "rf_batch_poll": (I, [P, ctypes.POINTER(I32)]),
 }
 
 _lib = None

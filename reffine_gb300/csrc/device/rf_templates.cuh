@@ -55,28 +55,33 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
         last = (ticket == (unsigned int)nunits - 1u);
     }
     __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (warp == 0) {
-        RfAcc tot;
-        rf_acc_init(P, tot);
-        for (int u = lane; u < nunits; u += 32) {
-            RfAcc p;
-            rf_ld_words(&p, (const RfAcc*)P.partials + u, (int)sizeof(RfAcc));
-            rf_acc_combine(tot, p);
-        }
+    if (last) {
+        __threadfence();
+        if (warp == 0) {
+            RfAcc tot;
+            rf_acc_init(P, tot);
+            for (int u = lane; u < nunits; u += 32) {
+                RfAcc p;
+                rf_ld_words(&p, (const RfAcc*)P.partials + u, (int)sizeof(RfAcc));
+                rf_acc_combine(tot, p);
+            }
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            RfAcc o = rf_acc_shfl(tot, off);
-            rf_acc_combine(tot, o);
-        }
-        if (lane == 0) {
-            rf_finish(P, tot, P.out);
-            *P.counter = 0u;
+            for (int off = 16; off > 0; off >>= 1) {
+                RfAcc o = rf_acc_shfl(tot, off);
+                rf_acc_combine(tot, o);
+            }
+            if (lane == 0) {
+                rf_finish(P, tot, P.out);
+                *P.counter = 0u;
+            }
         }
     }
+    __syncthreads();  // shared state is reused by the next work item of a persistent block
 }
 
+// Batched form: one persistent launch runs the work units of many queries of this shape.
+// work[w] = {query, unit}; params[query] is the query's parameter block.  A query's units are
+// the ones its stand-alone launch would run, folded in the same order: same bits either way.
 #define RF_SCAN_REDUCE_KERNEL(NAME, T)                                                      \
     extern "C" __global__ void __launch_bounds__(T) NAME(const __grid_constant__ RfParams P) \
     {                                                                                       \
@@ -84,6 +89,19 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
         rf_acc_init(P, acc);                                                                \
         rf_scan_reduce_rows<T>(P, blockIdx.x, gridDim.x, acc);                              \
         rf_scan_reduce_merge<T>(P, blockIdx.x, gridDim.x, acc);                             \
+    }                                                                                       \
+    extern "C" __global__ void __launch_bounds__(T)                                         \
+        rf_batch(const RfParams* __restrict__ params, const int2* __restrict__ work, const int* nwork) \
+    {                                                                                       \
+        const int n = *nwork;                                                               \
+        for (int w = blockIdx.x; w < n; w += gridDim.x) {                                   \
+            const int2 it = work[w];                                                        \
+            const RfParams& Q = params[it.x];                                               \
+            RfAcc acc;                                                                      \
+            rf_acc_init(Q, acc);                                                            \
+            rf_scan_reduce_rows<T>(Q, it.y, Q.nunits, acc);                                 \
+            rf_scan_reduce_merge<T>(Q, it.y, Q.nunits, acc);                                \
+        }                                                                                   \
     }
 #endif  // RF_SCAN_REDUCE
 
@@ -141,27 +159,38 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         last = (ticket == (unsigned int)nunits - 1u);
     }
     __syncthreads();
-    if (!last) return;
-    __threadfence();
-    for (int q = warp; q < Q; q += T / 32) {
-        const int m = q % RF_M;
-        unsigned long long a = rf_slot_init(P, m);
-        for (int u = lane; u < nunits; u += 32) a = rf_slot_combine(m, a, __ldcg(part + (long long)u * Q + q));
+    if (last) {
+        __threadfence();
+        for (int q = warp; q < Q; q += T / 32) {
+            const int m = q % RF_M;
+            unsigned long long a = rf_slot_init(P, m);
+            for (int u = lane; u < nunits; u += 32) a = rf_slot_combine(m, a, __ldcg(part + (long long)u * Q + q));
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) a = rf_slot_combine(m, a, __shfl_down_sync(0xffffffffu, a, off));
-        if (lane == 0) S[q] = a;
+            for (int off = 16; off > 0; off >>= 1) a = rf_slot_combine(m, a, __shfl_down_sync(0xffffffffu, a, off));
+            if (lane == 0) S[q] = a;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            rf_finish_groups(P, S, P.out);
+            *P.counter = 0u;
+        }
     }
-    __syncthreads();
-    if (tid == 0) {
-        rf_finish_groups(P, S, P.out);
-        *P.counter = 0u;
-    }
+    __syncthreads();  // shared state is reused by the next work item of a persistent block
 }
 
 #define RF_GROUP_REDUCE_KERNEL(NAME, T)                                                     \
     extern "C" __global__ void __launch_bounds__(T) NAME(const __grid_constant__ RfParams P) \
     {                                                                                       \
         rf_group_reduce<T>(P, blockIdx.x, gridDim.x);                                       \
+    }                                                                                       \
+    extern "C" __global__ void __launch_bounds__(T)                                         \
+        rf_batch(const RfParams* __restrict__ params, const int2* __restrict__ work, const int* nwork) \
+    {                                                                                       \
+        const int n = *nwork;                                                               \
+        for (int w = blockIdx.x; w < n; w += gridDim.x) {                                   \
+            const int2 it = work[w];                                                        \
+            rf_group_reduce<T>(params[it.x], it.y, params[it.x].nunits);                    \
+        }                                                                                   \
     }
 #endif  // RF_GROUP_REDUCE
 

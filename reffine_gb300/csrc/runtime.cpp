@@ -25,6 +25,7 @@
 #include "kernels.h"
 #include "lower.h"
 #include "rf_gpu.h"
+#include "objects.h"
 #include "runtime.h"
 
 namespace {
@@ -39,152 +40,13 @@ const char* k_params_src =
 #include "rf_params.h.inc"
     ;
 
-// ------------------------------------------------------------------------------------------
-// driver API entry points (resolved through the runtime, so the library does not link libcuda)
-// ------------------------------------------------------------------------------------------
-struct Driver {
-    CUresult (*ModuleLoadData)(CUmodule*, const void*) = nullptr;
-    CUresult (*ModuleUnload)(CUmodule) = nullptr;
-    CUresult (*ModuleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
-    CUresult (*LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
-                             CUstream, void**, void**) = nullptr;
-    CUresult (*FuncSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
-    CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
-    CUresult (*GetErrorString)(CUresult, const char**) = nullptr;
-    bool ok = false;
-    std::string err;
-};
-
-Driver& drv()
-{
-    static Driver d;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        auto get = [&](const char* name, void** fn) -> bool {
-            cudaDriverEntryPointQueryResult q;
-            cudaError_t e = cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q);
-            if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !*fn) {
-                d.err = std::string("driver entry point unavailable: ") + name;
-                return false;
-            }
-            return true;
-        };
-        d.ok = get("cuModuleLoadData", (void**)&d.ModuleLoadData) && get("cuModuleUnload", (void**)&d.ModuleUnload) &&
-               get("cuModuleGetFunction", (void**)&d.ModuleGetFunction) &&
-               get("cuLaunchKernel", (void**)&d.LaunchKernel) && get("cuFuncSetAttribute", (void**)&d.FuncSetAttribute) &&
-               get("cuOccupancyMaxActiveBlocksPerMultiprocessor", (void**)&d.OccupancyMaxActiveBlocksPerMultiprocessor) &&
-               get("cuGetErrorString", (void**)&d.GetErrorString);
-    });
-    return d;
-}
-
 }  // namespace
 
-// ------------------------------------------------------------------------------------------
-// objects
-// ------------------------------------------------------------------------------------------
-struct JitModule {
-    CUmodule mod = nullptr;
-    std::map<std::string, CUfunction> fns;
-    std::string log;
-    ~JitModule()
-    {
-        if (mod && drv().ok) drv().ModuleUnload(mod);
-    }
-};
-
-struct rf_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::mutex mu;
-    std::string err;
-    std::map<std::string, std::shared_ptr<JitModule>> modules;
-    std::atomic<long long> launches{0};
-    int sm_count = 0;
-    int* dev_err = nullptr;  // device error word shared by this context's launches
-};
-
-struct DevCol {
-    reffine::DataType type;
-    bool runend = false;
-    void* data = nullptr;             // values (run values)
-    long long nvals = 0;
-    unsigned short* valid = nullptr;  // validity of the values (NULL: all valid)
-    int* run_ends = nullptr;
-    long long logical = 0;            // rows
-    std::string name;
-    // allocations behind the pointers above (reused by repeated uploads into the same table)
-    void* data_buf = nullptr;
-    void* valid_buf = nullptr;
-    void* re_buf = nullptr;
-    size_t data_cap = 0, valid_cap = 0, re_cap = 0;
-};
-
-struct rf_table {
-    rf_ctx* ctx = nullptr;
-    long long dim = 1;
-    std::vector<DevCol> cols;
-    std::vector<char> present;        // column uploaded
-    long long* ix_slots = nullptr;
-    unsigned long long ix_cap = 0;
-    long long* ix_special = nullptr;
-    bool has_index = false;
-    long long null_count = 0;
-    std::string name;
-    std::vector<long long> ndv;       // cached distinct-count estimates per column (-1: unknown)
-};
-
-struct rf_plan {
-    rf_ctx* ctx = nullptr;
-    std::vector<rf_table*> staging;   // device copies of the host tables of thunk calls
-    rfg::Plan plan;
-    std::shared_ptr<JitModule> mod;
-    std::vector<CUfunction> fns;
-    void* partials = nullptr;
-    size_t partials_bytes = 0;
-    unsigned* counter = nullptr;
-    long long* range = nullptr;
-    unsigned char* dout = nullptr;
-    int max_units = 0;
-    int thunk_slot = -1;
-    // table outputs
-    void** d_ptrs = nullptr;          // device array: output column pointers, then bitmap pointers
-    long long* d_tiles = nullptr;     // per-tile counts / offsets
-    size_t tiles_cap = 0;
-    long long* d_res = nullptr;       // [rows written, null count]
-    // hash group-by
-    void* hg_keys = nullptr;
-    void* hg_acc = nullptr;
-    size_t hg_keys_cap = 0, hg_acc_cap = 0;
-    long long hg_retry_cap = 0;
-    // segmented reduce
-    long long* seg_woff = nullptr;
-    long long* seg_tmp = nullptr;
-    void* seg_part = nullptr;
-    size_t seg_runs_cap = 0, seg_part_cap = 0, seg_tmp_cap = 0;
-};
-
-namespace {
-// grows a device buffer to at least `bytes` (contents not kept)
-bool grow(void** buf, size_t* cap, size_t bytes, cudaStream_t s)
-{
-    if (*buf && *cap >= bytes) return true;
-    if (*buf) {
-        cudaStreamSynchronize(s);
-        cudaFree(*buf);
-    }
-    *buf = nullptr;
-    *cap = 0;
-    if (cudaMalloc(buf, bytes) != cudaSuccess) return false;
-    *cap = bytes;
-    return true;
-}
-}  // namespace
 
 // ------------------------------------------------------------------------------------------
 // helpers
 // ------------------------------------------------------------------------------------------
-namespace {
+namespace rfrt {
 
 int fail(rf_ctx* ctx, int code, const char* fmt, ...)
 {
@@ -197,19 +59,19 @@ int fail(rf_ctx* ctx, int code, const char* fmt, ...)
     return code;
 }
 
-#define CUDA_TRY(ctx, call)                                                                      \
-    do {                                                                                         \
-        cudaError_t e_ = (call);                                                                 \
-        if (e_ != cudaSuccess)                                                                   \
-            return fail(ctx, RF_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
-    } while (0)
-
 int cu_fail(rf_ctx* ctx, CUresult r, const char* what)
 {
     const char* s = "?";
     if (drv().GetErrorString) drv().GetErrorString(r, &s);
     return fail(ctx, RF_ERR_CUDA, "%s failed: %s", what, s);
 }
+
+}  // namespace rfrt
+
+using rfrt::cu_fail;
+using rfrt::fail;
+
+namespace {
 
 bool parse_format(const char* f, reffine::DataType& t)
 {
@@ -429,7 +291,7 @@ extern "C" int rf_ctx_stream(rf_ctx* ctx, void** stream)
     return RF_OK;
 }
 
-namespace {
+namespace rfrt {
 int check_device_error(rf_ctx* ctx)
 {
     int e = 0;
@@ -445,7 +307,8 @@ int check_device_error(rf_ctx* ctx)
     }
     return RF_OK;
 }
-}  // namespace
+}  // namespace rfrt
+using rfrt::check_device_error;
 
 extern "C" int rf_ctx_sync(rf_ctx* ctx)
 {
@@ -883,6 +746,23 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
         if (per_sm < 1) return fail(ctx, RF_ERR_JIT, "kernel %s cannot be resident (too many resources)", p->plan.kernels[i].name.c_str());
     }
     p->max_units = ctx->sm_count * per_sm;
+    if ((p->plan.kind == rfg::PlanKind::SCAN_REDUCE || p->plan.kind == rfg::PlanKind::GROUP_REDUCE) &&
+        !p->plan.device_range) {
+        const auto& mk = p->plan.kernels.back();
+        CUfunction bf;
+        if ((rc = get_function(ctx, *p->mod, "rf_batch", bf))) return rc;
+        if (mk.smem > 48 * 1024) {
+            CUresult cr = drv().FuncSetAttribute(bf, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)mk.smem);
+            if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "cuFuncSetAttribute");
+        }
+        int bps = 1;
+        CUresult cr = drv().OccupancyMaxActiveBlocksPerMultiprocessor(&bps, bf, mk.threads, mk.smem);
+        if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "occupancy query");
+        p->batch_fn = bf;
+        p->batch_grid = ctx->sm_count * std::max(1, bps);
+        p->batch_smem = mk.smem;
+        p->batch_threads = mk.threads;
+    }
     p->partials_bytes = (size_t)p->max_units * (p->plan.acc_bytes ? p->plan.acc_bytes : 8);
     CUDA_TRY(ctx, cudaMalloc(&p->partials, p->partials_bytes));
     CUDA_TRY(ctx, cudaMalloc((void**)&p->counter, 64));

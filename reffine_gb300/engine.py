@@ -263,6 +263,57 @@ class Plan:
         return p.value
 
 
+class Batch:
+    """Many Reduce queries in one launch per query shape (rf_batch_*).  add() returns the ctypes
+    struct that receives the query's result after wait()/poll()."""
+
+    def __init__(self, eng: Engine, capacity: int = 1024):
+        self.eng = eng
+        h = ctypes.c_void_p()
+        eng.check(eng.lib.rf_batch_create(eng.h, capacity, ctypes.byref(h)))
+        self.h = h
+        self.capacity = capacity
+        self._keep = []
+
+    def add(self, plan: "Plan", *inputs):
+        args = plan.args(*inputs)
+        out = plan.new_out()
+        self.eng.check(self.eng.lib.rf_batch_add(self.h, plan.h, args, len(inputs), ctypes.byref(out)))
+        self._keep.append((args, out))
+        return out
+
+    def __len__(self):
+        return len(self._keep)
+
+    def launch(self):
+        self.eng.check(self.eng.lib.rf_batch_launch(self.h, None))
+
+    def wait(self):
+        self.eng.check(self.eng.lib.rf_batch_wait(self.h))
+        return [from_c(o) for _, o in self._keep]
+
+    def poll(self) -> bool:
+        d = ctypes.c_int32()
+        self.eng.check(self.eng.lib.rf_batch_poll(self.h, ctypes.byref(d)))
+        return bool(d.value)
+
+    def reset(self):
+        self.eng.check(self.eng.lib.rf_batch_reset(self.h))
+        self._keep = []
+
+    def free(self):
+        if self.h:
+            self.eng.lib.rf_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            if self.eng.h:
+                self.free()
+        except Exception:
+            pass
+
+
 def check(fn: ir.Func, vectorize: bool = False) -> str:
     """Lowers and compiles a query for sm_103a without a device; returns the generated source."""
     lib = _capi.load()
