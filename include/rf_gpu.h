@@ -21,6 +21,7 @@
  *   rf_plan_thunk                   ExecEngine::Lookup<FnTy>(name) (include/reffine/engine/engine.h:61-66):
  *                                   a host function pointer with the generated function's signature
  *   rf_batch_*                      no counterpart: batching of many queries into one persistent launch
+ *   rf_server_*                     no counterpart: continuous-batching request loop
  *   rf_last_error                   no counterpart: the reference exits or aborts on errors
  *                                   (src/engine/cuda_engine.cpp:10-23)
  */
@@ -50,7 +51,8 @@ typedef enum rf_status {
     RF_ERR_JIT = 4,         /* NVRTC compile or module load error */
     RF_ERR_OOM = 5,         /* device or pinned-host allocation failed */
     RF_ERR_DEVICE = 6,      /* a kernel reported an error (bounded wait or probe ran out) */
-    RF_ERR_BUSY = 7         /* a batch or queue is full */
+    RF_ERR_BUSY = 7,        /* a batch or queue is full */
+    RF_ERR_CANCELLED = 8    /* a served request cancelled before it started */
 } rf_status;
 
 /* Argument of a plan run: a table or a scalar, in the Func's input order. */
@@ -164,14 +166,64 @@ int rf_batch_free(rf_batch* b);
 /* Adds a value-output run of `plan`; results land in host memory `host_out` after
  * rf_batch_wait.  Returns RF_ERR_BUSY when the batch is full. */
 int rf_batch_add(rf_batch* b, rf_plan* plan, const rf_arg* args, int32_t n_args, void* host_out);
-/* Launches everything added so far as one persistent kernel (captured in a CUDA graph and
- * replayed when the same set of plans recurs). */
+/* Launches everything added so far: one persistent kernel per query shape, in a CUDA graph
+ * built once per set of shapes and size class and replayed when it recurs.  Ordered after the
+ * work already queued on the context stream. */
 int rf_batch_launch(rf_batch* b, void* stream);
 int rf_batch_wait(rf_batch* b);
 /* Non-blocking: *done = 1 once the launched batch has finished (its results are then copied as
  * by rf_batch_wait), 0 while it runs. */
 int rf_batch_poll(rf_batch* b, int32_t* done);
 int rf_batch_reset(rf_batch* b);
+
+/* ---- serving: continuous batching over resident tables (no reference counterpart) ---------
+ * A server owns a scheduler thread.  Batched mode packs the pending Reduce queries into
+ * rf_batch launches on `lanes` streams as lanes free up (queries arriving while batches run
+ * are launched as soon as a lane is free) and runs table-result queries one at a time on a
+ * separate stream.  Per-query mode runs every request with rf_plan_run in arrival order (the
+ * baseline).  Requests are admitted while the device scratch in flight stays within
+ * hbm_budget_bytes; submit refuses with RF_ERR_BUSY once queue_capacity requests are pending.
+ * Tables and plans must outlive the requests that use them; indexes must be built beforehand. */
+typedef struct rf_server rf_server;
+enum { RF_SERVE_BATCHED = 0, RF_SERVE_PER_QUERY = 1 };
+typedef struct rf_server_config {
+    int32_t mode;             /* RF_SERVE_BATCHED or RF_SERVE_PER_QUERY */
+    int32_t max_batch;        /* queries per launch; 0: 256 */
+    int32_t lanes;            /* batches in flight at once; 0: 2 */
+    int32_t queue_capacity;   /* pending requests; 0: 65536 */
+    int64_t hbm_budget_bytes; /* device scratch in flight; 0: 8 GiB */
+} rf_server_config;
+typedef struct rf_completion {
+    uint64_t tag;             /* the submitter's tag */
+    int32_t status;           /* rf_status of the run */
+    int32_t batch_queries;    /* queries in the launch that carried it (1: alone) */
+    int64_t t_submit_ns, t_launch_ns, t_done_ns; /* rf_clock_ns() times */
+} rf_completion;
+typedef struct rf_server_stats {
+    int64_t submitted, completed, failed, cancelled, rejected;
+    int64_t batches, batched_queries;
+    int64_t queue_depth, max_queue_depth;
+    int64_t inflight_bytes, peak_inflight_bytes, inflight_queries;
+} rf_server_stats;
+int64_t rf_clock_ns(void); /* monotonic clock of the completion records */
+int rf_server_create(rf_ctx* ctx, const rf_server_config* cfg, rf_server** out);
+/* Queues a run of `plan`; its value result (or, for a table result, its rf_table*) is written
+ * to host_out before the completion with `tag` is delivered.  args are copied. */
+int rf_server_submit(rf_server* s, rf_plan* plan, const rf_arg* args, int32_t n_args, void* host_out, uint64_t tag);
+/* paused != 0: no queued request starts until resumed (requests on the GPU finish); submit,
+ * cancel and poll keep working.  For draining, and to hold a queue in a known state. */
+int rf_server_pause(rf_server* s, int32_t paused);
+/* Removes a request that has not started; it completes with RF_ERR_CANCELLED. */
+int rf_server_cancel(rf_server* s, uint64_t tag);
+/* Takes up to max completions, waiting up to timeout_us for the first. */
+int rf_server_poll(rf_server* s, rf_completion* out, int32_t max, int32_t* n_out, int32_t timeout_us);
+int rf_server_get_stats(rf_server* s, rf_server_stats* out);
+/* Pending requests complete as cancelled, work on the GPU finishes, then the server is freed. */
+int rf_server_free(rf_server* s);
+/* Open-loop load generator: submits request i at arrival_ns[i] after the call starts (tag i)
+ * and returns when all have completed, with records[i] = request i's completion. */
+int rf_server_replay(rf_server* s, int32_t n, rf_plan* const* plans, const rf_arg* const* args,
+                     const int32_t* n_args, void* const* outs, const int64_t* arrival_ns, rf_completion* records);
 
 #ifdef __cplusplus
 }

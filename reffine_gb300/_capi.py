@@ -12,9 +12,11 @@ from .table import ArrowArray, ArrowSchema
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "librf_gpu.so")
 
-RF_OK, RF_ERR_INVALID, RF_ERR_UNSUPPORTED, RF_ERR_CUDA, RF_ERR_JIT, RF_ERR_OOM, RF_ERR_DEVICE, RF_ERR_BUSY = range(8)
+(RF_OK, RF_ERR_INVALID, RF_ERR_UNSUPPORTED, RF_ERR_CUDA, RF_ERR_JIT, RF_ERR_OOM, RF_ERR_DEVICE, RF_ERR_BUSY,
+ RF_ERR_CANCELLED) = range(9)
 STATUS_NAMES = {0: "RF_OK", 1: "RF_ERR_INVALID", 2: "RF_ERR_UNSUPPORTED", 3: "RF_ERR_CUDA", 4: "RF_ERR_JIT",
-                5: "RF_ERR_OOM", 6: "RF_ERR_DEVICE", 7: "RF_ERR_BUSY"}
+                5: "RF_ERR_OOM", 6: "RF_ERR_DEVICE", 7: "RF_ERR_BUSY", 8: "RF_ERR_CANCELLED"}
+RF_SERVE_BATCHED, RF_SERVE_PER_QUERY = 0, 1
 RF_ARG_TABLE, RF_ARG_I64, RF_ARG_F64 = 0, 1, 2
 
 
@@ -27,6 +29,22 @@ class RfPlanInfo(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("n_inputs", ctypes.c_int32), ("output_is_table", ctypes.c_int32),
                 ("n_groups", ctypes.c_int32), ("output_size", ctypes.c_int64),
                 ("bytes_per_row", ctypes.c_int64 * 8), ("n_kernels", ctypes.c_int32), ("vectorize", ctypes.c_int32)]
+
+
+class RfServerConfig(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("max_batch", ctypes.c_int32), ("lanes", ctypes.c_int32),
+                ("queue_capacity", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64)]
+
+
+class RfCompletion(ctypes.Structure):
+    _fields_ = [("tag", ctypes.c_uint64), ("status", ctypes.c_int32), ("batch_queries", ctypes.c_int32),
+                ("t_submit_ns", ctypes.c_int64), ("t_launch_ns", ctypes.c_int64), ("t_done_ns", ctypes.c_int64)]
+
+
+class RfServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "submitted", "completed", "failed", "cancelled", "rejected", "batches", "batched_queries",
+        "queue_depth", "max_queue_depth", "inflight_bytes", "peak_inflight_bytes", "inflight_queries")]
 
 
 # every entry point of include/rf_gpu.h: name -> (restype, argtypes)
@@ -70,6 +88,16 @@ SIGNATURES = {
     "rf_batch_wait": (I, [P]),
     "rf_batch_reset": (I, [P]),
     "rf_batch_poll": (I, [P, ctypes.POINTER(I32)]),
+    "rf_clock_ns": (I64, []),
+    "rf_server_create": (I, [P, ctypes.POINTER(RfServerConfig), PP]),
+    "rf_server_submit": (I, [P, P, ctypes.POINTER(RfArg), I32, P, ctypes.c_uint64]),
+    "rf_server_cancel": (I, [P, ctypes.c_uint64]),
+    "rf_server_pause": (I, [P, I32]),
+    "rf_server_poll": (I, [P, ctypes.POINTER(RfCompletion), I32, ctypes.POINTER(I32), I32]),
+    "rf_server_get_stats": (I, [P, ctypes.POINTER(RfServerStats)]),
+    "rf_server_free": (I, [P]),
+    "rf_server_replay": (I, [P, I32, PP, ctypes.POINTER(ctypes.POINTER(RfArg)), ctypes.POINTER(I32), PP,
+                             ctypes.POINTER(I64), ctypes.POINTER(RfCompletion)]),
 }
 
 _lib = None

@@ -7,8 +7,8 @@
 // rf_batch kernel (device/rf_templates.cuh), a persistent kernel whose blocks walk a work list
 // of (query, unit) items; every query is cut into the units of its stand-alone launch and folded
 // in the same order, so each result has the same bits alone or in the mix.  The launch sequence
-// (parameter and work-list copies, counter reset, one kernel per shape, result copy) is captured
-// into a CUDA graph the first time a set of shapes is seen at a given size class and replayed
+// (parameter and work-list copies, counter reset, one kernel per shape, result copy) is built
+// as a CUDA graph the first time a set of shapes is seen at a given size class and replayed
 // afterwards.
 #include <cuda_runtime_api.h>
 
@@ -70,6 +70,7 @@ struct rf_batch {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     cudaEvent_t ctx_ready = nullptr;  // the context stream's work (uploads, index builds) so far
+    cudaStream_t last_stream = nullptr;  // the stream of the previous launch
     bool in_flight = false;
     size_t out_bytes = 0, counters_bytes = 0;
 };
@@ -78,14 +79,17 @@ using namespace rfrt;
 
 namespace {
 
-int grow_dev(rf_ctx* ctx, void** p, size_t* cap, size_t bytes)
+// Device buffers grow stream-ordered: the old one is released after the previous launch on
+// `last` (the stream that used it), the new one is ready in `s`'s order; no device-wide sync.
+int grow_dev(rf_ctx* ctx, void** p, size_t* cap, size_t bytes, cudaStream_t last, cudaStream_t s)
 {
     if (*p && *cap >= bytes) return RF_OK;
-    cudaStreamSynchronize(ctx->stream);
-    if (*p) cudaFree(*p);
+    if (*p) cudaFreeAsync(*p, last);
     *p = nullptr;
     *cap = 0;
-    if (cudaMalloc(p, bytes) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "batch device buffer (%zu bytes)", bytes);
+    bytes += bytes / 2;  // room to grow
+    if (cudaMallocAsync(p, bytes, s) != cudaSuccess)
+        return fail(ctx, RF_ERR_OOM, "batch device buffer (%zu bytes)", bytes);
     *cap = bytes;
     return RF_OK;
 }
@@ -96,6 +100,7 @@ int grow_host(rf_ctx* ctx, void** p, size_t* cap, size_t bytes)
     if (*p) cudaFreeHost(*p);
     *p = nullptr;
     *cap = 0;
+    bytes += bytes / 2;
     if (cudaHostAlloc(p, bytes, cudaHostAllocDefault) != cudaSuccess)
         return fail(ctx, RF_ERR_OOM, "batch pinned buffer (%zu bytes)", bytes);
     *cap = bytes;
@@ -190,11 +195,12 @@ extern "C" int rf_batch_launch(rf_batch* b, void* stream)
         it.group = f->second;
     }
     // scratch layout, fixed by the size class so a replayed graph copies the right ranges:
-    //   [ncls counters of 16 B][ncls result slots of OS B][partials of each query]
+    //   [error word, 16 B][ncls counters of 16 B][ncls result slots of OS B][partials of each query]
+    // The first two parts are zeroed and the first three copied back by every launch.
     size_t ncls = size_class(n);
     size_t os = 16;
     for (auto& it : b->items) os = std::max(os, size_class(it.plan->plan.out_size));
-    size_t counters_bytes = align_up(16 * ncls, 256);
+    size_t counters_bytes = align_up(16 + 16 * ncls, 256);
     size_t outs_base = counters_bytes;
     size_t off = outs_base + align_up(ncls * os, 256);
     for (size_t i = 0; i < n; i++) {
@@ -205,7 +211,8 @@ extern "C" int rf_batch_launch(rf_batch* b, void* stream)
     }
     size_t scratch_need = off;
     void* scr = b->d_scratch;
-    int rc = grow_dev(ctx, &scr, &b->scratch_cap, scratch_need);
+    cudaStream_t last = b->last_stream ? b->last_stream : s;
+    int rc = grow_dev(ctx, &scr, &b->scratch_cap, scratch_need, last, s);
     if (rc) return rc;
     if (scr != (void*)b->d_scratch) drop_graphs(b);
     b->d_scratch = (unsigned char*)scr;
@@ -224,7 +231,7 @@ extern "C" int rf_batch_launch(rf_batch* b, void* stream)
         words += 2 + size_class(groups[g].work.size() / 2) * 2;
     }
     void* w = b->d_work;
-    if ((rc = grow_dev(ctx, &w, &b->work_cap, words * 4))) return rc;
+    if ((rc = grow_dev(ctx, &w, &b->work_cap, words * 4, last, s))) return rc;
     if (w != (void*)b->d_work) drop_graphs(b);
     b->d_work = (int*)w;
     void* hw = b->h_work;
@@ -241,7 +248,8 @@ extern "C" int rf_batch_launch(rf_batch* b, void* stream)
     for (size_t i = 0; i < n; i++) {
         auto& it = b->items[i];
         RfParams P = it.P;
-        P.counter = (unsigned int*)(b->d_scratch + 16 * i);
+        P.counter = (unsigned int*)(b->d_scratch + 16 + 16 * i);
+        P.err = (int*)b->d_scratch;
         P.out = b->d_scratch + it.out_off;
         P.partials = b->d_scratch + it.part_off;
         P.range = nullptr;
@@ -250,7 +258,7 @@ extern "C" int rf_batch_launch(rf_batch* b, void* stream)
     b->out_bytes = ncls * os;
     b->counters_bytes = counters_bytes;
     void* ho = b->h_out;
-    if ((rc = grow_host(ctx, &ho, &b->h_out_cap, b->out_bytes + 256))) return rc;
+    if ((rc = grow_host(ctx, &ho, &b->h_out_cap, counters_bytes + b->out_bytes))) return rc;
     if (ho != (void*)b->h_out) drop_graphs(b);
     b->h_out = (unsigned char*)ho;
     // graph: signature = shapes + size classes (copies are sized to the class)
@@ -260,41 +268,61 @@ extern "C" int rf_batch_launch(rf_batch* b, void* stream)
                std::to_string(size_class(groups[g].work.size() / 2));
     auto gi = b->graphs.find(sig);
     if (gi == b->graphs.end()) {
+        // built node by node (no stream capture, which would interact with other threads'
+        // synchronising calls): three setup nodes, one kernel node per shape (the shapes run
+        // concurrently), then the copy of error word, counters and results back to the host
         cudaGraph_t graph;
-        CUDA_TRY(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        cudaMemcpyAsync(b->d_params, b->h_params, sizeof(RfParams) * std::min(ncls, (size_t)b->cap),
-                        cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync(b->d_work, b->h_work, words * 4, cudaMemcpyHostToDevice, s);
-        cudaMemsetAsync(b->d_scratch, 0, counters_bytes, s);
-        for (size_t g = 0; g < groups.size(); g++) {
+        CUDA_TRY(ctx, cudaGraphCreate(&graph, 0));
+        cudaGraphNode_t setup[3], out_node;
+        std::vector<cudaGraphNode_t> kn(groups.size());
+        cudaMemsetParams ms{};
+        ms.dst = b->d_scratch;
+        ms.value = 0;
+        ms.elementSize = 1;
+        ms.width = counters_bytes;
+        ms.height = 1;
+        cudaError_t e = cudaGraphAddMemcpyNode1D(&setup[0], graph, nullptr, 0, b->d_params, b->h_params,
+                                                 sizeof(RfParams) * std::min(ncls, (size_t)b->cap),
+                                                 cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaGraphAddMemcpyNode1D(&setup[1], graph, nullptr, 0, b->d_work, b->h_work, words * 4,
+                                         cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaGraphAddMemsetNode(&setup[2], graph, nullptr, 0, &ms);
+        CUresult cr = CUDA_SUCCESS;
+        for (size_t g = 0; g < groups.size() && e == cudaSuccess && cr == CUDA_SUCCESS; g++) {
             const RfParams* pp = b->d_params;
             const int* wl = b->d_work + goff[g] + 2;
             const int* nw = b->d_work + goff[g];
             void* kargs[] = {&pp, &wl, &nw};
-            int grid = std::max(1, std::min(groups[g].grid, (int)size_class(groups[g].work.size() / 2)));
-            CUresult cr = drv().LaunchKernel(groups[g].fn, grid, 1, 1, groups[g].threads, 1, 1, (unsigned)groups[g].smem,
-                                             (CUstream)s, kargs, nullptr);
-            if (cr != CUDA_SUCCESS) {
-                cudaStreamEndCapture(s, &graph);
-                return cu_fail(ctx, cr, "batch kernel launch (capture)");
-            }
+            CUDA_KERNEL_NODE_PARAMS kp{};
+            kp.func = groups[g].fn;
+            kp.gridDimX = (unsigned)std::max(1, std::min(groups[g].grid, (int)size_class(groups[g].work.size() / 2)));
+            kp.gridDimY = kp.gridDimZ = 1;
+            kp.blockDimX = (unsigned)groups[g].threads;
+            kp.blockDimY = kp.blockDimZ = 1;
+            kp.sharedMemBytes = (unsigned)groups[g].smem;
+            kp.kernelParams = kargs;
+            cr = drv().GraphAddKernelNode((CUgraphNode*)&kn[g], (CUgraph)graph, (const CUgraphNode*)setup, 3, &kp);
         }
-        cudaMemcpyAsync(b->h_out, b->d_scratch + counters_bytes, b->out_bytes, cudaMemcpyDeviceToHost, s);
-        CUDA_TRY(ctx, cudaStreamEndCapture(s, &graph));
-        cudaGraphExec_t exec;
-        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e == cudaSuccess && cr == CUDA_SUCCESS)
+            e = cudaGraphAddMemcpyNode1D(&out_node, graph, kn.data(), kn.size(), b->h_out, b->d_scratch,
+                                         counters_bytes + b->out_bytes, cudaMemcpyDeviceToHost);
+        cudaGraphExec_t exec = nullptr;
+        if (e == cudaSuccess && cr == CUDA_SUCCESS) e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return fail(ctx, RF_ERR_CUDA, "graph instantiation: %s", cudaGetErrorString(e));
+        if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "batch graph kernel node");
+        if (e != cudaSuccess) return fail(ctx, RF_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
         gi = b->graphs.emplace(sig, exec).first;
     }
-    // the batch runs after everything already queued on the context stream (table uploads and
-    // the index builds rf_batch_add may have enqueued)
+    // the batch runs after everything already queued on the context stream (table uploads,
+    // stream-ordered allocations, the index builds rf_batch_add may have enqueued)
     if (s != ctx->stream) {
         CUDA_TRY(ctx, cudaEventRecord(b->ctx_ready, ctx->stream));
         CUDA_TRY(ctx, cudaStreamWaitEvent(s, b->ctx_ready, 0));
     }
     CUDA_TRY(ctx, cudaGraphLaunch(gi->second, s));
     CUDA_TRY(ctx, cudaEventRecord(b->done, s));
+    b->last_stream = s;
     ctx->launches += (long long)groups.size();
     b->in_flight = true;
     b->groups_plan.clear();
@@ -309,10 +337,11 @@ extern "C" int rf_batch_wait(rf_batch* b)
     if (!b->in_flight) return RF_OK;
     CUDA_TRY(ctx, cudaEventSynchronize(b->done));
     b->in_flight = false;
-    int rc = check_device_error(ctx);
-    if (rc) return rc;
+    int e = 0;
+    std::memcpy(&e, b->h_out, sizeof(int));
+    if (e) return fail(ctx, RF_ERR_DEVICE, "device error %d in a batched query", e);
     for (auto& it : b->items)
-        if (it.host_out) std::memcpy(it.host_out, b->h_out + (it.out_off - b->counters_bytes), it.plan->plan.out_size);
+        if (it.host_out) std::memcpy(it.host_out, b->h_out + it.out_off, it.plan->plan.out_size);
     return RF_OK;
 }
 

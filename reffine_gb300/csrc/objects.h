@@ -28,6 +28,9 @@ struct Driver {
     CUresult (*LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
                              CUstream, void**, void**) = nullptr;
     CUresult (*FuncSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*FuncGetAttribute)(int*, CUfunction_attribute, CUfunction) = nullptr;
+    CUresult (*GraphAddKernelNode)(CUgraphNode*, CUgraph, const CUgraphNode*, size_t,
+                                   const CUDA_KERNEL_NODE_PARAMS*) = nullptr;
     CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
     CUresult (*GetErrorString)(CUresult, const char**) = nullptr;
     bool ok = false;
@@ -51,6 +54,8 @@ inline Driver& drv()
         d.ok = get("cuModuleLoadData", (void**)&d.ModuleLoadData) && get("cuModuleUnload", (void**)&d.ModuleUnload) &&
                get("cuModuleGetFunction", (void**)&d.ModuleGetFunction) &&
                get("cuLaunchKernel", (void**)&d.LaunchKernel) && get("cuFuncSetAttribute", (void**)&d.FuncSetAttribute) &&
+               get("cuFuncGetAttribute", (void**)&d.FuncGetAttribute) &&
+               get("cuGraphAddKernelNode", (void**)&d.GraphAddKernelNode) &&
                get("cuOccupancyMaxActiveBlocksPerMultiprocessor", (void**)&d.OccupancyMaxActiveBlocksPerMultiprocessor) &&
                get("cuGetErrorString", (void**)&d.GetErrorString);
     });
@@ -79,6 +84,7 @@ struct rf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::mutex mu;
+    std::mutex err_mu;                // guards err (written by any thread that fails)
     std::string err;
     std::map<std::string, std::shared_ptr<JitModule>> modules;
     std::atomic<long long> launches{0};
@@ -129,6 +135,7 @@ struct rf_plan {
     unsigned char* dout = nullptr;
     int max_units = 0;
     int thunk_slot = -1;
+    unsigned char* h_res = nullptr;   // pinned: [error word, 16 B][value result]
     // batched execution (value-output plans without device-computed loop bounds)
     CUfunction batch_fn = nullptr;
     int batch_grid = 0;
@@ -137,7 +144,7 @@ struct rf_plan {
     // table outputs
     void** d_ptrs = nullptr;          // device array: output column pointers, then bitmap pointers
     long long* d_tiles = nullptr;     // per-tile counts / offsets
-    size_t tiles_cap = 0;
+    size_t tiles_cap = 0;             // bytes
     long long* d_res = nullptr;       // [rows written, null count]
     // hash group-by
     void* hg_keys = nullptr;
@@ -152,17 +159,17 @@ struct rf_plan {
 };
 
 namespace {
-// grows a device buffer to at least `bytes` (contents not kept)
+// Grows a device buffer to at least `bytes` (contents not kept), stream-ordered on `s`: the old
+// buffer is released after the work already queued on `s`, and nothing synchronises the device
+// (a cudaFree would stall every stream, including other threads' batches).  The buffer must be
+// used on `s` only, or after the caller has synchronised with `s`.
 bool grow(void** buf, size_t* cap, size_t bytes, cudaStream_t s)
 {
     if (*buf && *cap >= bytes) return true;
-    if (*buf) {
-        cudaStreamSynchronize(s);
-        cudaFree(*buf);
-    }
+    if (*buf) cudaFreeAsync(*buf, s);
     *buf = nullptr;
     *cap = 0;
-    if (cudaMalloc(buf, bytes) != cudaSuccess) return false;
+    if (cudaMallocAsync(buf, bytes, s) != cudaSuccess) return false;
     *cap = bytes;
     return true;
 }
@@ -173,6 +180,7 @@ namespace rfrt {
 int launch(rf_ctx* ctx, CUfunction f, int grid, int block, size_t smem, cudaStream_t s, RfParams* P);
 int fail(rf_ctx* ctx, int code, const char* fmt, ...);
 int check_device_error(rf_ctx* ctx);
+int device_error(rf_ctx* ctx, int e);  // RF_OK for 0, else clears the context's error word and fails
 int cu_fail(rf_ctx* ctx, CUresult r, const char* what);
 }  // namespace rfrt
 

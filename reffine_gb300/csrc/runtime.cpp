@@ -55,7 +55,10 @@ int fail(rf_ctx* ctx, int code, const char* fmt, ...)
     va_start(ap, fmt);
     vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
-    if (ctx) ctx->err = buf;
+    if (ctx) {
+        std::lock_guard<std::mutex> g(ctx->err_mu);
+        ctx->err = buf;
+    }
     return code;
 }
 
@@ -282,7 +285,15 @@ extern "C" int rf_gpu_shutdown(rf_ctx* ctx)
     return RF_OK;
 }
 
-extern "C" const char* rf_last_error(rf_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+extern "C" const char* rf_last_error(rf_ctx* ctx)
+{
+    // a copy per calling thread: the server's threads may fail while a client reads the message
+    static thread_local std::string msg;
+    if (!ctx) return "no context";
+    std::lock_guard<std::mutex> g(ctx->err_mu);
+    msg = ctx->err;
+    return msg.c_str();
+}
 
 extern "C" int rf_ctx_stream(rf_ctx* ctx, void** stream)
 {
@@ -296,6 +307,11 @@ int check_device_error(rf_ctx* ctx)
 {
     int e = 0;
     CUDA_TRY(ctx, cudaMemcpy(&e, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+    return device_error(ctx, e);
+}
+
+int device_error(rf_ctx* ctx, int e)
+{
     if (e) {
         cudaMemset(ctx->dev_err, 0, sizeof(int));
         const char* what = e == RF_DEVERR_PROBE ? "hash probe exhausted the table"
@@ -730,7 +746,7 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
             continue;
         }
         if ((rc = get_function(ctx, *p->mod, k.name, f))) return rc;
-        if (k.smem > 48 * 1024) {
+        if (k.smem > 0) {  // the default cap is 48 KiB minus the kernel's static shared memory
             CUresult cr = drv().FuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)k.smem);
             if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "cuFuncSetAttribute");
         }
@@ -743,7 +759,18 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
         CUresult cr = drv().OccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fns[i], p->plan.kernels[i].threads,
                                                                       p->plan.kernels[i].smem);
         if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "occupancy query");
-        if (per_sm < 1) return fail(ctx, RF_ERR_JIT, "kernel %s cannot be resident (too many resources)", p->plan.kernels[i].name.c_str());
+        if (per_sm < 1) {
+            int regs = -1, ssm = -1, maxt = -1, maxdyn = -1;
+            drv().FuncGetAttribute(&regs, CU_FUNC_ATTRIBUTE_NUM_REGS, p->fns[i]);
+            drv().FuncGetAttribute(&ssm, CU_FUNC_ATTRIBUTE_SHARED_SIZE_BYTES, p->fns[i]);
+            drv().FuncGetAttribute(&maxt, CU_FUNC_ATTRIBUTE_MAX_THREADS_PER_BLOCK, p->fns[i]);
+            drv().FuncGetAttribute(&maxdyn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, p->fns[i]);
+            return fail(ctx, RF_ERR_JIT,
+                        "kernel %s cannot be resident: %d threads, %zu B dynamic shared memory (allowed %d), %d B "
+                        "static, %d registers, at most %d threads",
+                        p->plan.kernels[i].name.c_str(), p->plan.kernels[i].threads, p->plan.kernels[i].smem, maxdyn,
+                        ssm, regs, maxt);
+        }
     }
     p->max_units = ctx->sm_count * per_sm;
     if ((p->plan.kind == rfg::PlanKind::SCAN_REDUCE || p->plan.kind == rfg::PlanKind::GROUP_REDUCE) &&
@@ -751,7 +778,7 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
         const auto& mk = p->plan.kernels.back();
         CUfunction bf;
         if ((rc = get_function(ctx, *p->mod, "rf_batch", bf))) return rc;
-        if (mk.smem > 48 * 1024) {
+        if (mk.smem > 0) {
             CUresult cr = drv().FuncSetAttribute(bf, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)mk.smem);
             if (cr != CUDA_SUCCESS) return cu_fail(ctx, cr, "cuFuncSetAttribute");
         }
@@ -824,6 +851,7 @@ extern "C" int rf_plan_free(rf_plan* p)
     cudaFree(p->seg_woff);
     cudaFree(p->seg_tmp);
     cudaFree(p->seg_part);
+    cudaFreeHost(p->h_res);
     for (auto* t : p->staging)
         if (t) {
             free_table_mem(t);
@@ -1004,17 +1032,17 @@ int ndv_estimate(rf_table* t, int col, cudaStream_t s, long long* out)
     }
     DevCol& dc = t->cols[col];
     unsigned* regs = nullptr;
-    CUDA_TRY(ctx, cudaMalloc((void**)&regs, RF_HLL_M * sizeof(unsigned)));
+    CUDA_TRY(ctx, cudaMallocAsync((void**)&regs, RF_HLL_M * sizeof(unsigned), s));
     int e = rf_k_hll(dc.data, dc.valid, dc.nvals, regs, s);
     if (e) {
-        cudaFree(regs);
+        cudaFreeAsync(regs, s);
         return fail(ctx, RF_ERR_CUDA, "distinct-count sketch launch: %s", cudaGetErrorString((cudaError_t)e));
     }
     ctx->launches += 1;
     std::vector<unsigned> h(RF_HLL_M);
     cudaError_t ce = cudaMemcpyAsync(h.data(), regs, RF_HLL_M * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(regs, s);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
-    cudaFree(regs);
     if (ce != cudaSuccess) return fail(ctx, RF_ERR_CUDA, "distinct-count sketch: %s", cudaGetErrorString(ce));
     double sum = 0, m = RF_HLL_M;
     int zeros = 0;
@@ -1099,12 +1127,8 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         }
     }
     long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
-    if ((size_t)std::max<long long>(ntiles, 1) > p->tiles_cap) {
-        cudaStreamSynchronize(s);
-        cudaFree(p->d_tiles);
-        p->tiles_cap = (size_t)std::max<long long>(ntiles, 1024);
-        if (cudaMalloc((void**)&p->d_tiles, p->tiles_cap * 8) != cudaSuccess) {
-            p->tiles_cap = 0;
+    if ((size_t)std::max<long long>(ntiles, 1) * 8 > p->tiles_cap) {  // tiles_cap: bytes
+        if (!grow((void**)&p->d_tiles, &p->tiles_cap, (size_t)std::max<long long>(ntiles, 1024) * 8, s)) {
             free_table_mem(t.get());
             return fail(ctx, RF_ERR_OOM, "tile buffer allocation failed");
         }
@@ -1256,9 +1280,19 @@ extern "C" int rf_plan_run(rf_plan* p, const rf_arg* args, int32_t n_args, void*
         *(rf_table**)out = nullptr;
         return run_table(p, args, n_args, (rf_table**)out, s);
     }
+    if (!p->h_res) {
+        if (cudaHostAlloc((void**)&p->h_res, 16 + p->plan.out_size, cudaHostAllocDefault) != cudaSuccess)
+            return fail(ctx, RF_ERR_OOM, "pinned result buffer");
+    }
     int rc = enqueue(p, args, n_args, s, nullptr);
     if (rc) return rc;
-    if (out) CUDA_TRY(ctx, cudaMemcpyAsync(out, p->dout, p->plan.out_size, cudaMemcpyDeviceToHost, s));
+    // the error word and the result come back in one round trip
+    CUDA_TRY(ctx, cudaMemcpyAsync(p->h_res, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaMemcpyAsync(p->h_res + 16, p->dout, p->plan.out_size, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(ctx, cudaStreamSynchronize(s));
-    return check_device_error(ctx);
+    int e;
+    memcpy(&e, p->h_res, sizeof(int));
+    if ((rc = device_error(ctx, e))) return rc;
+    if (out) memcpy(out, p->h_res + 16, p->plan.out_size);
+    return RF_OK;
 }

@@ -26,7 +26,7 @@ def declared_functions():
             continue
         text = open(os.path.join(inc, f)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        for m in re.finditer(r"^\s*(?:int|const char\*)\s+(rf_\w+)\s*\(", text, flags=re.M):
+        for m in re.finditer(r"^\s*(?:int|int64_t|const char\*)\s+(rf_\w+)\s*\(", text, flags=re.M):
             names.add(m.group(1))
     return names
 

@@ -59,6 +59,16 @@ def test_join_parity(eng):
     assert sum(g[1] for g in ref) > 0
 
 
+@pytest.mark.parametrize("groups", [1, 11, 12, 25])
+def test_join_group_counts(eng, groups):
+    # 12 groups x 2 aggregates x 256 threads x 8 B is exactly 48 KiB of privatised slots: the
+    # kernel must opt in to more than the default dynamic shared memory (48 KiB minus static)
+    b, p = W.join_tables(20_000, 400_003, seed=12)
+    fn = W.join_query(b.get_data_type(), p.get_data_type(), groups, 100, 900)
+    got = eng.compile(fn).run(eng.upload(b).build_index(), eng.upload(p))
+    assert_same(got, loopgen.Query(fn)(b, p))
+
+
 def test_validity_of_column_one_gates_rows(eng):
     # loopgen.cpp:238: a SubVector reduce skips rows whose column-1 value is null
     t = W.filter_sum_table(100_000, seed=3)
