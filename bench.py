@@ -13,6 +13,9 @@ GB/s = algorithmic bytes (each referenced column read once) / time.
              copies of the referenced columns and the device->host result copy inside the timing
   roofline   achieved algorithmic GB/s of the main kernel against the measured HBM copy peak
   cpu_baseline  the oracle (Reffine's CPU loop restated, g++ -O3, one core) on the same table
+  serving    10k requests over resident tables of log-uniform size, Poisson arrivals: the
+             continuous-batching server against per-query launches on the same GPU (p50/p99
+             latency, queries/s, GB/s), every result checked against the query run alone
 
 --impl reference times the oracle port alone (the reference's CPU path; it is single-threaded).
 Multi-GPU (torchrun): each rank scans its own partition (weak scaling), no collective on the
@@ -247,6 +250,46 @@ def _cols_read_cpu(fn, input_idx):
     return sorted({int(c) for c in re.findall(r"P\.t\[%d\]\.col\[(\d+)\]" % slot, src)})
 
 
+def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5)):
+    """Batched serving over resident tables (config 4): the same Poisson request stream through
+    the continuous-batching server and through per-query launches (one rf_plan_run per request,
+    in arrival order) on the same GPU.  Rates are fractions of the per-query path's closed-loop
+    capacity.  Every result is compared with the query run alone."""
+    import math
+    from reffine_gb300 import serve
+    t0 = time.perf_counter()
+    wl = serve.build_workload(eng, n_queries=n_queries, max_rows=max_rows)
+    t_build = time.perf_counter() - t0
+    tab = [i for i, r in enumerate(wl.requests) if r.plan.info.output_is_table]
+    sample = set(tab[:: max(1, len(tab) // 40)])  # ~40 table results compared in full, all by row count
+    alone = serve.run_alone(eng, wl.requests, sample)
+    keep = ("qps", "gbps", "p50_us", "p99_us", "mean_us", "mean_batch", "failed", "mismatches")
+    slim = lambda d: {k: (round(d[k], 3) if isinstance(d[k], float) else d[k]) for k in keep}
+    out = {"queries": len(wl.requests),
+           "shapes": dict(zip(serve.SHAPES, np.bincount([r.shape for r in wl.requests], minlength=4).tolist())),
+           "table_rows": "log-uniform in [1e3, %.0e], 6 tables per shape, resident" % max_rows,
+           "resident_gb": round(wl.resident_bytes / 1e9, 2),
+           "bytes_per_query_mb": round(sum(r.nbytes for r in wl.requests) / len(wl.requests) / 1e6, 2),
+           "server": "2 lanes x 256 queries per launch, 8 GiB scratch budget", "workload_build_s": round(t_build, 1),
+           "check": "value results bit for bit; table results by row count, %d of them key-sorted in full "
+                    "(FP64 within 1e-12)" % len(sample)}
+    closed = {}
+    for mode in ("per_query", "batched"):
+        closed[mode] = slim(serve.serve_run(eng, wl, mode, math.inf, alone, check_tables=True))
+    out["closed_loop"] = closed
+    cap = closed["per_query"]["qps"]
+    sweep = []
+    for f in rates:
+        row = {"rate_qps": round(cap * f, 1), "of_per_query_capacity": f}
+        for mode in ("per_query", "batched"):
+            row[mode] = slim(serve.serve_run(eng, wl, mode, cap * f, alone, seed=40 + int(f * 10)))
+        sweep.append(row)
+    out["poisson"] = sweep
+    runs = [closed[m] for m in closed] + [r[m] for r in sweep for m in ("per_query", "batched")]
+    out["identical_to_alone"] = all(r["mismatches"] == 0 and r["failed"] == 0 for r in runs)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -257,6 +300,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--rows", type=int, default=0, help="override the row count (profiling a smaller case)")
+    ap.add_argument("--serving-queries", type=int, default=10_000,
+                    help="requests of the batched-serving comparison (0: skip it)")
+    ap.add_argument("--serving-max-rows", type=int, default=50_000_000)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -374,6 +420,13 @@ def main():
         cpu, _ = cpu_baseline(rfn, rtabs, nbytes, note="" if args.config != 2 else
                               "; keys pre-sorted and run-end encoded (the reference's grouped form), sort not timed")
 
+    serving = None
+    if rank == 0 and args.serving_queries > 0 and world == 1:
+        try:
+            serving = bench_serving(eng, args.serving_queries, args.serving_max_rows)
+        except Exception as ex:  # report, do not hide
+            serving = {"error": str(ex)[:300]}
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -385,7 +438,7 @@ def main():
                              "kernel": {1: "rf_main (scan-reduce)", 2: "rf_main (grouped scan-reduce)",
                                         5: "rf_hg_agg + materialisation (hash group-by)"}.get(plan.kind, str(plan.kind)),
                              "algorithmic_bytes_per_launch": nbytes},
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(l1 - l0), "clocks": clk,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(l1 - l0), "clocks": clk, "serving": serving,
                 "result_sample": ("%d output rows" % out_rows[0]) if table_out else str(engine.from_c(out_check))[:200]}
         print(json.dumps(line), flush=True)
     eng.close()

@@ -192,6 +192,8 @@ typedef struct rf_server_config {
     int32_t lanes;            /* batches in flight at once; 0: 2 */
     int32_t queue_capacity;   /* pending requests; 0: 65536 */
     int64_t hbm_budget_bytes; /* device scratch in flight; 0: 8 GiB */
+    int32_t lane_share_pct;   /* a lane's launch fills at most this % of the block slots; 0: 75 */
+    int32_t reserved_;
 } rf_server_config;
 typedef struct rf_completion {
     uint64_t tag;             /* the submitter's tag */

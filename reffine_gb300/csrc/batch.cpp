@@ -71,6 +71,7 @@ struct rf_batch {
     cudaEvent_t done = nullptr;
     cudaEvent_t ctx_ready = nullptr;  // the context stream's work (uploads, index builds) so far
     cudaStream_t last_stream = nullptr;  // the stream of the previous launch
+    int share_pct = 100;              // at most this share of a shape's resident blocks per launch
     bool in_flight = false;
     size_t out_bytes = 0, counters_bytes = 0;
 };
@@ -296,7 +297,8 @@ extern "C" int rf_batch_launch(rf_batch* b, void* stream)
             void* kargs[] = {&pp, &wl, &nw};
             CUDA_KERNEL_NODE_PARAMS kp{};
             kp.func = groups[g].fn;
-            kp.gridDimX = (unsigned)std::max(1, std::min(groups[g].grid, (int)size_class(groups[g].work.size() / 2)));
+            int cap = std::max(1, groups[g].grid * b->share_pct / 100);
+            kp.gridDimX = (unsigned)std::max(1, std::min(cap, (int)size_class(groups[g].work.size() / 2)));
             kp.gridDimY = kp.gridDimZ = 1;
             kp.blockDimX = (unsigned)groups[g].threads;
             kp.blockDimY = kp.blockDimZ = 1;
@@ -361,6 +363,17 @@ extern "C" int rf_batch_poll(rf_batch* b, int32_t* done)
     *done = 1;
     return rf_batch_wait(b);
 }
+
+namespace rfrt {
+// A launch of this batch fills at most `pct` percent of the block slots its kernels could hold,
+// leaving the rest of every SM to batches launched beside it.  The grid only changes which
+// block runs a work item, not the items or their fold order, so results are unchanged.
+void batch_set_share(rf_batch* b, int pct)
+{
+    b->share_pct = std::min(100, std::max(1, pct));
+    drop_graphs(b);
+}
+}  // namespace rfrt
 
 extern "C" int rf_batch_reset(rf_batch* b)
 {

@@ -181,6 +181,7 @@ int launch(rf_ctx* ctx, CUfunction f, int grid, int block, size_t smem, cudaStre
 int fail(rf_ctx* ctx, int code, const char* fmt, ...);
 int check_device_error(rf_ctx* ctx);
 int device_error(rf_ctx* ctx, int e);  // RF_OK for 0, else clears the context's error word and fails
+void batch_set_share(rf_batch* b, int pct);
 int cu_fail(rf_ctx* ctx, CUresult r, const char* what);
 }  // namespace rfrt
 

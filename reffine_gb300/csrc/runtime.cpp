@@ -1103,28 +1103,41 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     t->cols.resize(nc);
     t->present.assign(nc, 1);
     std::vector<void*> hptrs(2 * RF_MAX_COLS, nullptr);
-    for (size_t c = 0; c < nc; c++) {
-        DevCol& dc = t->cols[c];
-        dc.type = pl.out_cols[c];
-        dc.name = (c < (size_t)pl.out_dim ? "it" : "out") + std::to_string(c < (size_t)pl.out_dim ? c : c - pl.out_dim);
-        size_t bytes = (size_t)std::max<long long>(cap, 1) * dc.type.size();
-        if (cudaMallocAsync(&dc.data_buf, bytes + 16, s) != cudaSuccess) {
-            free_table_mem(t.get());
-            return fail(ctx, RF_ERR_OOM, "output column allocation (%zu bytes) failed", bytes);
-        }
-        dc.data_cap = bytes;
-        dc.data = dc.data_buf;
-        hptrs[c] = dc.data_buf;
-        if (pl.vectorize) {
-            size_t vb = (size_t)((std::max<long long>(cap, 1) + 31) / 32) * 4;
-            if (cudaMallocAsync(&dc.valid_buf, vb + 16, s) != cudaSuccess) {
-                free_table_mem(t.get());
-                return fail(ctx, RF_ERR_OOM, "output bitmap allocation failed");
+    // output columns of `rows` rows (validity bitmaps when vectorised)
+    auto alloc_cols = [&](long long rows) -> int {
+        for (size_t c = 0; c < nc; c++) {
+            DevCol& dc = t->cols[c];
+            dc.type = pl.out_cols[c];
+            dc.name = (c < (size_t)pl.out_dim ? "it" : "out") +
+                      std::to_string(c < (size_t)pl.out_dim ? c : c - pl.out_dim);
+            size_t bytes = (size_t)std::max<long long>(rows, 1) * dc.type.size();
+            if (cudaMallocAsync(&dc.data_buf, bytes + 16, s) != cudaSuccess)
+                return fail(ctx, RF_ERR_OOM, "output column allocation (%zu bytes) failed", bytes);
+            dc.data_cap = bytes;
+            dc.data = dc.data_buf;
+            hptrs[c] = dc.data_buf;
+            if (pl.vectorize) {
+                size_t vb = (size_t)((std::max<long long>(rows, 1) + 31) / 32) * 4;
+                if (cudaMallocAsync(&dc.valid_buf, vb + 16, s) != cudaSuccess)
+                    return fail(ctx, RF_ERR_OOM, "output bitmap allocation failed");
+                dc.valid_cap = vb;
+                CUDA_TRY(ctx, cudaMemsetAsync(dc.valid_buf, 0, vb + 16, s));
+                hptrs[RF_MAX_COLS + c] = dc.valid_buf;
             }
-            dc.valid_cap = vb;
-            CUDA_TRY(ctx, cudaMemsetAsync(dc.valid_buf, 0, vb + 16, s));
-            hptrs[RF_MAX_COLS + c] = dc.valid_buf;
         }
+        CUDA_TRY(ctx, cudaMemcpyAsync(p->d_ptrs, hptrs.data(), sizeof(void*) * hptrs.size(), cudaMemcpyHostToDevice, s));
+        return RF_OK;
+    };
+    // A compacting materialisation (count, scan, scatter) learns its row count from the scan: the
+    // columns are then allocated at exactly that size before the scatter, so an output holds its
+    // rows, not the loop's range (a hash group-by's slot table is ~2.2x the distinct keys).  A
+    // vectorised one writes every visited element and is allocated at the range up front.
+    int iscatter = -1;
+    for (size_t i = 0; i < pl.kernels.size(); i++)
+        if (pl.kernels[i].role == rfg::KernelSpec::SCATTER && !pl.vectorize) iscatter = (int)i;
+    if (iscatter < 0 && (rc = alloc_cols(cap))) {
+        free_table_mem(t.get());
+        return rc;
     }
     long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
     if ((size_t)std::max<long long>(ntiles, 1) * 8 > p->tiles_cap) {  // tiles_cap: bytes
@@ -1133,7 +1146,6 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
             return fail(ctx, RF_ERR_OOM, "tile buffer allocation failed");
         }
     }
-    CUDA_TRY(ctx, cudaMemcpyAsync(p->d_ptrs, hptrs.data(), sizeof(void*) * hptrs.size(), cudaMemcpyHostToDevice, s));
     CUDA_TRY(ctx, cudaMemsetAsync(p->d_res, 0, 64, s));
     P.aux0 = p->d_ptrs;
     P.aux1 = p->d_ptrs + RF_MAX_COLS;
@@ -1158,6 +1170,29 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     P.nunits = units;
     for (size_t i = 0; i < pl.kernels.size(); i++) {
         const auto& k = pl.kernels[i];
+        if ((int)i == iscatter) {
+            long long total = 0;
+            CUDA_TRY(ctx, cudaMemcpyAsync(&total, p->d_res, 8, cudaMemcpyDeviceToHost, s));
+            CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            if ((rc = check_device_error(ctx))) {
+                free_table_mem(t.get());
+                if (pl.kind == rfg::PlanKind::HASH_GROUP && rc == RF_ERR_DEVICE && hg_cap < (1LL << 34) &&
+                    std::string(rf_last_error(ctx)).find("capacity") != std::string::npos) {
+                    p->hg_retry_cap = hg_cap * 2;  // the estimate was low: grow and rerun
+                    return run_table(p, args, n_args, out, s);
+                }
+                return rc;
+            }
+            if (total < 0 || total > cap) {
+                free_table_mem(t.get());
+                return fail(ctx, RF_ERR_DEVICE, "materialisation counted %lld rows of %lld", total, cap);
+            }
+            if ((rc = alloc_cols(total))) {
+                free_table_mem(t.get());
+                return rc;
+            }
+            cap = total;
+        }
         if (k.role == rfg::KernelSpec::SEGSCAN) {
             int e = rf_k_scan_excl(p->seg_woff, nruns, p->seg_tmp, s);
             if (e) {
@@ -1188,7 +1223,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     if (rc) {
         free_table_mem(t.get());
         if (pl.kind == rfg::PlanKind::HASH_GROUP && rc == RF_ERR_DEVICE && hg_cap < (1LL << 34) &&
-            ctx->err.find("capacity") != std::string::npos) {
+            std::string(rf_last_error(ctx)).find("capacity") != std::string::npos) {
             p->hg_retry_cap = hg_cap * 2;  // the estimate was low: grow and rerun
             return run_table(p, args, n_args, out, s);
         }

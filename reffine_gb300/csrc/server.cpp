@@ -297,6 +297,7 @@ extern "C" int rf_server_create(rf_ctx* ctx, const rf_server_config* cfg, rf_ser
     if (c.lanes > 16) c.lanes = 16;
     if (c.queue_capacity <= 0) c.queue_capacity = 1 << 16;
     if (c.hbm_budget_bytes <= 0) c.hbm_budget_bytes = (int64_t)8 << 30;
+    if (c.lane_share_pct <= 0 || c.lane_share_pct > 100) c.lane_share_pct = 75;
     if (c.mode != RF_SERVE_BATCHED && c.mode != RF_SERVE_PER_QUERY)
         return fail(ctx, RF_ERR_INVALID, "unknown serving mode %d", c.mode);
     S->cfg = c;
@@ -309,6 +310,7 @@ extern "C" int rf_server_create(rf_ctx* ctx, const rf_server_config* cfg, rf_ser
                     if (l2.batch) rf_batch_free(l2.batch);
                 return rc;
             }
+            batch_set_share(ln.batch, c.lane_share_pct);
             CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking));
         }
     }

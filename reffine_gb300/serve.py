@@ -31,12 +31,13 @@ class Server:
     """A running rf_server (its scheduler threads live in the library)."""
 
     def __init__(self, eng: Engine, mode: str = "batched", max_batch: int = 256, lanes: int = 2,
-                 queue_capacity: int = 1 << 16, hbm_budget_bytes: int = 8 << 30):
+                 queue_capacity: int = 1 << 16, hbm_budget_bytes: int = 8 << 30, lane_share_pct: int = 75):
         self.eng = eng
         cfg = _capi.RfServerConfig()
         cfg.mode = {"batched": _capi.RF_SERVE_BATCHED, "per_query": _capi.RF_SERVE_PER_QUERY}[mode]
         cfg.max_batch, cfg.lanes, cfg.queue_capacity, cfg.hbm_budget_bytes = max_batch, lanes, queue_capacity, \
             hbm_budget_bytes
+        cfg.lane_share_pct = lane_share_pct
         h = ctypes.c_void_p()
         eng.check(eng.lib.rf_server_create(eng.h, ctypes.byref(cfg), ctypes.byref(h)))
         self.h = h
@@ -224,14 +225,28 @@ def canonical(eng: Engine, plan: Plan, h) -> Dict:
     return {"cols": [c[order] for c in cols], "len": out["len"]}
 
 
-def run_alone(eng: Engine, reqs: Sequence[Request]) -> list:
-    """Every request run by itself (rf_plan_run): the reference results of the mixed runs."""
+def table_rows(eng: Engine, h) -> int:
+    n = ctypes.c_int64()
+    eng.check(eng.lib.rf_table_num_rows(ctypes.c_void_p(h), ctypes.byref(n)))
+    return n.value
+
+
+def run_alone(eng: Engine, reqs: Sequence[Request], table_sample: Optional[set] = None) -> list:
+    """Every request run by itself (rf_plan_run): the reference results of the mixed runs.  A
+    value result is kept as its bytes; a table result as its key-sorted export when its index is
+    in `table_sample` (None: all), else as its row count."""
     res = []
-    for r in reqs:
+    for i, r in enumerate(reqs):
         o = new_outs([r])[0]
         args = r.plan.args(*r.inputs)
         eng.check(eng.lib.rf_plan_run(r.plan.h, args, len(r.inputs), ctypes.byref(o), None))
-        res.append(canonical(eng, r.plan, o.value) if r.plan.info.output_is_table else bytes(o))
+        if not r.plan.info.output_is_table:
+            res.append(bytes(o))
+        elif table_sample is None or i in table_sample:
+            res.append(canonical(eng, r.plan, o.value))
+        else:
+            res.append(table_rows(eng, o.value))
+            DeviceTable(eng, ctypes.c_void_p(o.value), r.plan.fn.output.type, []).free()
     return res
 
 
@@ -248,19 +263,22 @@ def tables_close(a: Dict, b: Dict, rtol: float = 1e-12) -> bool:
 
 
 def compare(eng: Engine, reqs: Sequence[Request], outs: list, alone: list, check_tables: bool = True) -> int:
-    """Mismatches of a mixed run against the results alone: value results bit for bit, table
+    """Mismatches of a mixed run against the results alone: value results bit for bit; table
     results key-sorted with FP64 columns within 1e-12 relative (a hash group-by adds each key's
-    rows in arrival order at the slot, which varies run to run).  Frees the table results."""
+    rows in arrival order at the slot, which varies run to run) where the alone result was kept
+    whole, else by row count.  Frees the table results."""
     bad = 0
     for r, o, a in zip(reqs, outs, alone):
         if r.plan.info.output_is_table:
             if not o.value:
                 bad += 1
                 continue
-            if check_tables:
+            if isinstance(a, dict) and check_tables:
                 bad += not tables_close(canonical(eng, r.plan, o.value), a)
-            else:
-                DeviceTable(eng, ctypes.c_void_p(o.value), r.plan.fn.output.type, []).free()
+                continue
+            n = table_rows(eng, o.value)
+            bad += n != (a["len"] if isinstance(a, dict) else a)
+            DeviceTable(eng, ctypes.c_void_p(o.value), r.plan.fn.output.type, []).free()
         else:
             bad += bytes(o) != a
     return bad
@@ -297,6 +315,13 @@ def serve_run(eng: Engine, wl: Workload, mode: str, rate_qps: float, alone: list
     finally:
         srv.close()
     summ = latency_summary(rec)
+    shapes = np.array([r.shape for r in reqs])
+    summ["by_shape"] = {SHAPES[k]: latency_summary(rec[shapes == k]) for k in sorted(set(shapes.tolist()))}
+    bad = rec["status"] != 0
+    summ["failures"] = {"%s:%s" % (SHAPES[k], _capi.STATUS_NAMES.get(int(st), st)): int(c)
+                        for (k, st), c in zip(*np.unique(np.stack([shapes[bad], rec["status"][bad]], 1), axis=0,
+                                                         return_counts=True))} if bad.any() else {}
+    summ["last_error"] = eng.lib.rf_last_error(eng.h).decode(errors="replace")[:200] if bad.any() else ""
     span = (rec["t_done_ns"].max() - rec["t_submit_ns"].min()) / 1e9
     summ["gbps"] = sum(r.nbytes for r in reqs) / span / 1e9 if span > 0 else None
     summ["mismatches"] = compare(eng, reqs, outs, alone, check_tables)
