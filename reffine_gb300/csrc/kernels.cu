@@ -197,7 +197,26 @@ __global__ void __launch_bounds__(512) hll_kernel(const long long* __restrict__ 
         if (r[i]) atomicMax(&regs[i], r[i]);
 }
 
+// the m sampled rows are i * n / m; a null key samples as RF_EMPTY_KEY
+__global__ void __launch_bounds__(256) sample_kernel(const long long* __restrict__ keys, const unsigned short* __restrict__ valid,
+                                                     long long n, long long m, long long* __restrict__ out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+        const long long r = i * n / m;
+        out[i] = rf_valid(valid, r) ? __ldg(keys + r) : RF_EMPTY_KEY;
+    }
+}
+
 }  // namespace
+
+extern "C" int rf_k_sample_keys(const void* keys, const unsigned short* valid, long long n, long long m, long long* out,
+                                cudaStream_t stream)
+{
+    if (m <= 0 || n <= 0) return 0;
+    const int blocks = (int)std::min<long long>((m + 255) / 256, 1024);
+    sample_kernel<<<blocks, 256, 0, stream>>>(static_cast<const long long*>(keys), valid, n, m, out);
+    return (int)cudaGetLastError();
+}
 
 extern "C" int rf_k_hll(const void* keys, const unsigned short* valid, long long n, unsigned* regs, cudaStream_t stream)
 {

@@ -19,6 +19,10 @@ int rf_k_scan_excl(long long* data, long long n, long long* tmp, cudaStream_t st
 #define RF_HLL_M 16384
 int rf_k_hll(const void* keys, const unsigned short* valid, long long n, unsigned* regs, cudaStream_t stream);
 
+// m keys of an int64 column sampled at rows i * n / m (null keys as RF_EMPTY_KEY), 1 launch.
+int rf_k_sample_keys(const void* keys, const unsigned short* valid, long long n, long long m, long long* out,
+                     cudaStream_t stream);
+
 // Device address (with the calling thread's current device = `device`) and size of the fixed
 // scratch array of rf_plan_run_noalloc.  The address is looked up once per device.
 int rf_k_noalloc_scratch(int device, void** ptr, size_t* bytes);

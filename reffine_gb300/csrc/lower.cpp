@@ -1825,15 +1825,23 @@ private:
         for (size_t i = 0; i < leaves.size(); i++)
             if (leaves[i].op != AggOp::NONE) act.push_back((int)i);
         const int L = (int)act.size();
-        const int S = std::max(256, std::min(1024, (int)(24 * 1024 / (8 * (L + 1)))));
+        // shared-memory tiers of the aggregation kernel (see rf_hg_agg below): HK hottest keys
+        // with warp-private accumulators, WK further hot keys with block-shared accumulators
+        // the aggregation kernel's hottest keys (see rf_hg_agg below): HK keys with warp-private
+        // accumulators, at most 16 KB of them per block
+        const int HT = 256, HW = HT / 32, LL = std::max(L, 1);
+        int HK = 128;
+        while (HK > 8 && HW * HK * LL * 8 > 16 * 1024) HK /= 2;
+        plan_.hg_hot = HK;
+        plan_.hg_warm = 0;
         std::string sl = std::to_string(d.slot);
         std::string c0 = "P.t[" + sl + "].col[0]";
         std::ostringstream o;
         o << "// generated by the reffine_gb300 lowering pass: " << fn_->name << " (hash group-by)\n";
         const int SW = L + 1 <= 4 ? 4 : (L + 1 <= 8 ? 8 : 16);
         if (L + 1 > 16) throw LowerError("hash group-by with more than 15 aggregates");
-        o << "#include \"rf_device.cuh\"\n\n#define RF_HG_L " << std::max(L, 1) << "\n#define RF_HG_S " << S
-          << "\n#define RF_HG_SW " << SW << "\n\n";
+        o << "#include \"rf_device.cuh\"\n\n#define RF_HG_L " << LL << "\n#define RF_HG_SW " << SW
+          << "\n#define RF_HG_T " << HT << "\n#define RF_HG_HK " << HK << "\n\n";
         plan_.acc_bytes = (size_t)SW * 8;
         auto kind_of = [&](const Leaf& lf) -> std::string {
             bool f = lf.type.is_float() && !lf.count;
@@ -1869,19 +1877,24 @@ private:
             for (auto& dcl : Ei.decls) o << "    " << dcl << "\n";
             o << "    switch (l) {\n" << b.str() << "    default: return 0ULL;\n    }\n}\n\n";
         }
-        // one row's contribution to the accumulators of its group (slot A, leaf stride `st`)
+        // One row's contribution: the columns it reads are loaded first into a row struct
+        // (rf_hg_load, so a thread issues the loads of several rows before using any of them),
+        // then added to a slot's accumulators (rf_hg_apply: slot A, leaf stride `st`, atomics) or
+        // returned as values (rf_hg_vals: the identity where the row adds nothing, for the
+        // warp-level fold of the hottest keys).
         {
+            const DataType& vt = fn_->inputs[d.input]->type;
+            auto bind_row_struct = [&](Emitter& E) {
+                Val v;
+                v.k = Val::STRUCT;
+                v.type = red.val->type;
+                for (size_t c = 1; c < vt.dtypes.size(); c++) v.f.push_back(E.scalar("R.v" + std::to_string(c), vt.dtypes[c]));
+                E.bind(red.val, v);
+            };
             Emitter E(*this);
             bind_inputs(E);
-            const DataType& vt = fn_->inputs[d.input]->type;
-            Val v;
-            v.k = Val::STRUCT;
-            v.type = red.val->type;
-            for (size_t c = 1; c < vt.dtypes.size(); c++)
-                v.f.push_back(E.scalar("rf_ld<" + ctype(vt.dtypes[c]) + ">(P.t[" + sl + "].col[" + std::to_string(c) + "].data, r)",
-                                       vt.dtypes[c]));
-            E.bind(red.val, v);
-            std::ostringstream u;
+            bind_row_struct(E);
+            std::ostringstream u, xv;
             for (int k = 0; k < L; k++) {
                 auto& lf = leaves[act[k]];
                 std::string cond = lf.cond ? E.ev(order_conjuncts(lf.cond)).c : "";
@@ -1890,11 +1903,47 @@ private:
                 if (kind_of(lf) == "fmax" || kind_of(lf) == "fmin") call = "if (!" + call + ") rf_set_err(P, RF_DEVERR_WAIT)";
                 if (!cond.empty()) u << "    if (" << cond << ") { " << call << "; }\n";
                 else u << "    " << call << ";\n";
+                std::string x = enc(lf, val);
+                if (!cond.empty()) xv << "    x[" << k << "] = (" << cond << ") ? " << x << " : rf_hg_identity(P, " << k << ");\n";
+                else xv << "    x[" << k << "] = " << x << ";\n";
             }
-            o << "RF_DEV void rf_hg_apply(const RfParams& P, long long r, unsigned long long* A, long long st)\n{\n";
+            std::string body = u.str() + xv.str();
+            for (auto& dcl : E.decls) body += dcl;
+            // the row struct holds exactly the columns the contribution reads
+            o << "struct RfHgRow {\n    bool ok;\n";
+            std::ostringstream ld;
+            ld << "RF_DEV void rf_hg_load(const RfParams& P, long long r, RfHgRow& R)\n{\n";
+            ld << "    R.ok = rf_valid(P.t[" << sl << "].col[1].valid, r);  // loopgen.cpp:238\n";
+            for (size_t c = 1; c < vt.dtypes.size(); c++) {
+                std::string f = "R.v" + std::to_string(c);
+                bool used = false;
+                for (size_t pos = body.find(f); pos != std::string::npos; pos = body.find(f, pos + 1)) {
+                    char nx = pos + f.size() < body.size() ? body[pos + f.size()] : ' ';
+                    if (!isdigit((unsigned char)nx)) used = true;
+                }
+                if (!used) continue;
+                o << "    " << ctype(vt.dtypes[c]) << " v" << c << ";\n";
+                ld << "    " << f << " = rf_ld<" << ctype(vt.dtypes[c]) << ">(P.t[" << sl << "].col[" << c << "].data, r);\n";
+            }
+            o << "};\n\n" << ld.str() << "}\n\n";
+            o << "RF_DEV void rf_hg_apply(const RfParams& P, const RfHgRow& R, unsigned long long* A, long long st)\n{\n";
+            o << "    if (!R.ok) return;\n";
             for (auto& dcl : E.decls) o << "    " << dcl << "\n";
-            o << "    if (!rf_valid(P.t[" << sl << "].col[1].valid, r)) return;  // loopgen.cpp:238\n";
             o << u.str() << "    (void)A; (void)st;\n}\n\n";
+            o << "RF_DEV void rf_hg_vals(const RfParams& P, const RfHgRow& R, unsigned long long* x)\n{\n";
+            o << "    if (!R.ok) {\n        for (int l = 0; l < RF_HG_L; l++) x[l] = rf_hg_identity(P, l);\n        return;\n    }\n";
+            for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+            o << xv.str() << "}\n\n";
+            o << "RF_DEV unsigned long long rf_hg_comb(int l, unsigned long long a, unsigned long long b)\n{\n    switch (l) {\n";
+            for (int k = 0; k < L; k++) {
+                auto& lf = leaves[act[k]];
+                std::string ct = lf.count ? "long long"
+                                 : (lf.op == AggOp::OR || lf.op == AggOp::AND) ? "long long" : acc_ctype(lf);
+                bool f = lf.type.is_float() && !lf.count;
+                std::string A = f ? "rf_u2f(a)" : "(" + ct + ")(a)", B = f ? "rf_u2f(b)" : "(" + ct + ")(b)";
+                o << "        case " << k << ": return " << enc(lf, combine_expr(lf, A, B)) << ";\n";
+            }
+            o << "        default: return a;\n    }\n}\n\n";
         }
         // flush of a pre-aggregated slot into the global table
         o << "RF_DEV void rf_hg_merge(const RfParams& P, unsigned long long* A, long long st, const unsigned long long* B, long long bst)\n{\n";
@@ -1906,7 +1955,24 @@ private:
             o << "    " << call << ";\n";
         }
         o << "    (void)A; (void)B; (void)st; (void)bst;\n}\n\n";
-        o << R"(// slot of `key` in the global table (claimed if new); C + 1 slots, slot C is the empty key's
+        o << R"(// slot of `key` in the global table from probe position h on (claimed if new): one
+// compare-and-swap per probe, which claims an empty slot or finds the key in one round trip
+// (hot keys never come here, so the slots are not contended)
+RF_DEV long long rf_hg_slot_from(const RfParams& P, long long key, unsigned long long h, unsigned long long n0)
+{
+    unsigned long long* tab = (unsigned long long*)P.aux4;
+    const unsigned long long C = (unsigned long long)P.aux_n1;
+    for (unsigned long long n = 0; n < n0; ++n) {
+        const unsigned long long old =
+            atomicCAS(tab + h * RF_HG_SW, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)key);
+        if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) return (long long)h;
+        if (++h == C) h = 0;
+    }
+    rf_set_err(P, RF_DEVERR_OVERFLOW);
+    return -1;
+}
+
+// slot of `key` in the global table (claimed if new); C + 1 slots, slot C is the empty key's
 RF_DEV long long rf_hg_slot(const RfParams& P, long long key)
 {
     unsigned long long* tab = (unsigned long long*)P.aux4;
@@ -1915,13 +1981,52 @@ RF_DEV long long rf_hg_slot(const RfParams& P, long long key)
         if (tab[C * RF_HG_SW] == 0) atomicExch(tab + C * RF_HG_SW, 1ULL);
         return (long long)C;
     }
+    return rf_hg_slot_from(P, key, rf_home(key, C), C);
+}
+
+extern "C" __global__ void __launch_bounds__(256) rf_hg_init(const __grid_constant__ RfParams P)
+{
+    unsigned long long* tab = (unsigned long long*)P.aux4;
+    const long long C = P.aux_n1;
+    // word by word, so a warp's stores are contiguous
+    const long long words = (C + 1) * RF_HG_SW;
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < words; w += (long long)gridDim.x * blockDim.x) {
+        const long long s = w / RF_HG_SW;
+        const int f = (int)(w % RF_HG_SW);
+        tab[w] = f == 0 ? (s < C ? (unsigned long long)RF_EMPTY_KEY : 0ULL)
+                        : (f <= RF_HG_L ? rf_hg_identity(P, f - 1) : 0ULL);
+    }
+}
+
+// Aggregation.  Rows of the hottest keys (chosen from a sample of the key column, so Zipf-like
+// skew lands here) fold inside each warp: the lanes holding the same hot key find each other
+// with __match_any_sync, the lowest of them folds their contributions and adds them, without
+// atomics, to the warp's own accumulators.  All other rows go to the global table, whose
+// accumulators take fire-and-forget atomics; its keys are read through L1 first (a claimed
+// slot's key never changes; a stale empty is corrected by the compare-and-swap).  The hot-key
+// index is a read-only table built on the host: open addressing, load <= 0.5, 32-bit
+// multiplicative hash of the folded key.
+// Dynamic shared memory:
+//   hk[2HK] i64 | hid[2HK] i32 | wacc[W][HK][L] | xs[W][32][L] | seen[HK] u8
+// (a key is a group as soon as one valid row has it, whatever the row adds)
+RF_DEV unsigned rf_hg_h32(long long key, int bits)
+{
+    const unsigned f = (unsigned)key ^ (unsigned)((unsigned long long)key >> 32);
+    return (f * 0x9E3779B1u) >> (32 - bits);
+}
+
+RF_DEV long long rf_hg_slot_l1(const RfParams& P, long long key)
+{
+    unsigned long long* tab = (unsigned long long*)P.aux4;
+    const unsigned long long C = (unsigned long long)P.aux_n1;
+    if (key == RF_EMPTY_KEY) return rf_hg_slot(P, key);
     unsigned long long h = rf_home(key, C);
     for (unsigned long long n = 0; n < C; ++n) {
         unsigned long long* kp = tab + h * RF_HG_SW;
-        unsigned long long cur = __ldcg(kp);
+        const unsigned long long cur = __ldca(kp);
         if (cur == (unsigned long long)key) return (long long)h;
         if (cur == (unsigned long long)RF_EMPTY_KEY) {
-            unsigned long long old = atomicCAS(kp, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)key);
+            const unsigned long long old = atomicCAS(kp, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)key);
             if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) return (long long)h;
         }
         if (++h == C) h = 0;
@@ -1930,77 +2035,92 @@ RF_DEV long long rf_hg_slot(const RfParams& P, long long key)
     return -1;
 }
 
-extern "C" __global__ void __launch_bounds__(256) rf_hg_init(const __grid_constant__ RfParams P)
+extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_constant__ RfParams P)
 {
-    unsigned long long* tab = (unsigned long long*)P.aux4;
-    const long long C = P.aux_n1;
-    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s <= C; s += (long long)gridDim.x * blockDim.x) {
-        unsigned long long* sl = tab + s * RF_HG_SW;
-        sl[0] = s < C ? (unsigned long long)RF_EMPTY_KEY : 0ULL;
-        for (int l = 0; l < RF_HG_L; l++) sl[1 + l] = rf_hg_identity(P, l);
+    constexpr int W = RF_HG_T / 32, HKS = 2 * RF_HG_HK;
+    int bits = 0;
+    while ((1 << bits) < HKS) bits++;
+    extern __shared__ __align__(16) unsigned char smem[];
+    long long* hk = (long long*)smem;
+    int* hid = (int*)(hk + HKS);
+    unsigned long long* wacc = (unsigned long long*)(smem + ((size_t)HKS * 12 + 15) / 16 * 16);
+    unsigned long long* xs = wacc + (size_t)W * RF_HG_HK * RF_HG_L;
+    unsigned char* seen = (unsigned char*)(xs + (size_t)W * 32 * RF_HG_L);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // the hot-key image: hk | hid (aux5; null: no hot keys)
+    const unsigned char* img = (const unsigned char*)P.aux5;
+    for (int i = tid; i < HKS; i += RF_HG_T) {
+        hk[i] = img ? ((const long long*)img)[i] : RF_EMPTY_KEY;
+        hid[i] = img ? ((const int*)(img + HKS * 8))[i] : 0;
     }
-}
-
-extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constant__ RfParams P)
-{
-    __shared__ long long sk[RF_HG_S];
-    __shared__ unsigned long long sv[RF_HG_L * RF_HG_S];
-    for (int i = threadIdx.x; i < RF_HG_S; i += blockDim.x) {
-        sk[i] = RF_EMPTY_KEY;
-        for (int l = 0; l < RF_HG_L; l++) sv[i * RF_HG_L + l] = rf_hg_identity(P, l);
-    }
+    for (int i = tid; i < W * RF_HG_HK * RF_HG_L; i += RF_HG_T) wacc[i] = rf_hg_identity(P, i % RF_HG_L);
+    for (int i = tid; i < RF_HG_HK; i += RF_HG_T) seen[i] = 0;
     __syncthreads();
     unsigned long long* tab = (unsigned long long*)P.aux4;
+    unsigned long long* wa = wacc + (size_t)warp * RF_HG_HK * RF_HG_L;
+    unsigned long long* x = xs + ((size_t)warp * 32 + lane) * RF_HG_L;
     const long long n = P.aux_n0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    // four rows per thread per step: their key loads are issued together
-    for (long long r0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; r0 < n; r0 += 4 * stride) {
-        long long kk[4];
-        bool ok[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            long long r = r0 + j * stride;
+    // whole warps step together (the fold needs every lane); rows past the end are inactive
+    const long long wstride = (long long)gridDim.x * RF_HG_T;
+    for (long long base = ((long long)blockIdx.x * W + warp) * 32; base < n; base += wstride) {
+        const long long r = base + lane;
 )";
-        o << "            ok[j] = r < n && rf_valid(" << c0 << ".valid, r);  // a null key is no group\n";
-        o << "            kk[j] = r < n ? rf_ld<int64_t>(" << c0 << ".data, r) : 0;\n        }\n";
-        o << R"(#pragma unroll 1
-        for (int j = 0; j < 4; j++) {
-        if (!ok[j]) continue;
-        const long long r = r0 + j * stride, key = kk[j];
-        unsigned long long* A = nullptr;
-        if (key != RF_EMPTY_KEY) {
-            // read-only probe first; claim a free slot only when the probe reaches one
-            unsigned h = (unsigned)rf_home(key, RF_HG_S);
-            for (int p = 0; p < 8; p++) {
-                long long cur = ((volatile long long*)sk)[h];
+        o << "        const bool act = r < n && rf_valid(" << c0 << ".valid, r);  // a null key is no group\n";
+        o << "        const long long key = act ? rf_ld<int64_t>(" << c0 << ".data, r) : RF_EMPTY_KEY;\n";
+        o << R"(        RfHgRow row;
+        if (act) rf_hg_load(P, r, row);
+        int h = -1;
+        if (act && key != RF_EMPTY_KEY) {
+            unsigned q = rf_hg_h32(key, bits);
+            for (int p = 0; p < HKS; p++) {
+                const long long cur = hk[q];
                 if (cur == key) {
-                    A = sv + h * RF_HG_L;
+                    h = hid[q];
                     break;
                 }
-                if (cur == RF_EMPTY_KEY) {
-                    unsigned long long old = atomicCAS((unsigned long long*)&sk[h], (unsigned long long)RF_EMPTY_KEY,
-                                                       (unsigned long long)key);
-                    if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key) {
-                        A = sv + h * RF_HG_L;
-                        break;
-                    }
-                }
-                if (++h == RF_HG_S) h = 0;
+                if (cur == RF_EMPTY_KEY) break;
+                q = (q + 1) & (HKS - 1);
             }
         }
-        if (!A) {
-            long long g = rf_hg_slot(P, key);
-            if (g < 0) continue;
-            A = tab + g * RF_HG_SW + 1;
-        }
-        rf_hg_apply(P, r, A, 1);
+        // fold of the hottest keys: lanes of one hot key find each other, the lowest folds
+        const unsigned peers = __match_any_sync(0xffffffffu, h >= 0 ? h : -1 - lane);
+        if (h >= 0) {
+            rf_hg_vals(P, row, x);
+            __syncwarp(peers);
+            if (lane == __ffs(peers) - 1) {
+                unsigned long long a[RF_HG_L];
+#pragma unroll
+                for (int l = 0; l < RF_HG_L; l++) a[l] = x[l];
+                for (unsigned m = peers & (peers - 1); m; m &= m - 1) {
+                    const unsigned long long* y = xs + ((size_t)warp * 32 + (__ffs(m) - 1)) * RF_HG_L;
+#pragma unroll
+                    for (int l = 0; l < RF_HG_L; l++) a[l] = rf_hg_comb(l, a[l], y[l]);
+                }
+                unsigned long long* A = wa + (size_t)h * RF_HG_L;
+#pragma unroll
+                for (int l = 0; l < RF_HG_L; l++) A[l] = rf_hg_comb(l, A[l], a[l]);
+                seen[h] = 1;
+            }
+            __syncwarp(peers);
+        } else if (act) {
+            const long long g = rf_hg_slot_l1(P, key);
+            if (g >= 0) rf_hg_apply(P, row, tab + g * RF_HG_SW + 1, 1);
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < RF_HG_S; i += blockDim.x) {
-        if (sk[i] == RF_EMPTY_KEY) continue;
-        long long g = rf_hg_slot(P, sk[i]);
-        if (g >= 0) rf_hg_merge(P, tab + g * RF_HG_SW + 1, 1, sv + i * RF_HG_L, 1);
+    // warp accumulators of each hottest key, folded over the warps, then into the global table
+    for (int i = tid; i < HKS; i += RF_HG_T) {
+        if (hk[i] == RF_EMPTY_KEY) continue;
+        const int id = hid[i];
+        if (!seen[id]) continue;
+        unsigned long long a[RF_HG_L];
+#pragma unroll
+        for (int l = 0; l < RF_HG_L; l++) a[l] = wacc[(size_t)id * RF_HG_L + l];
+        for (int w2 = 1; w2 < W; w2++)
+#pragma unroll
+            for (int l = 0; l < RF_HG_L; l++) a[l] = rf_hg_comb(l, a[l], wacc[((size_t)w2 * RF_HG_HK + id) * RF_HG_L + l]);
+        const long long g = rf_hg_slot(P, hk[i]);
+        if (g >= 0) rf_hg_merge(P, tab + g * RF_HG_SW + 1, 1, a, 1);
     }
 }
 
@@ -2078,7 +2198,11 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_agg(const __grid_constan
         o << "RF_MATERIALIZE_KERNELS(" << T << ", " << plan_.out_cols.size() << ")\n";
         plan_.kernels.clear();
         plan_.kernels.push_back({"rf_hg_init", 256, 0, KernelSpec::INIT});
-        plan_.kernels.push_back({"rf_hg_agg", 256, 0, KernelSpec::MAIN});
+        {
+            const size_t head = ((size_t)2 * HK * 12 + 15) / 16 * 16;
+            const size_t smem = head + ((size_t)HW * HK + (size_t)HW * 32) * LL * 8 + (size_t)(HK + 15) / 16 * 16;
+            plan_.kernels.push_back({"rf_hg_agg", HT, smem, KernelSpec::MAIN});
+        }
         plan_.kernels.push_back({"rf_count", T, 0, KernelSpec::COUNT});
         plan_.kernels.push_back({"rf_scan", 1024, 0, KernelSpec::SCAN});
         plan_.kernels.push_back({"rf_scatter", T, 0, KernelSpec::SCATTER});

@@ -80,6 +80,8 @@ struct Plan {
     bool out_is_table = false;
     size_t acc_bytes = 0;               // bytes of one unit's partial (scan-reduce, segmented reduce)
     int seg_chunk = 256;                // segmented reduce: rows per chunk
+    int hg_hot = 0;                     // hash group-by: hottest keys folded per warp (index 2x)
+    int hg_warm = 0;                    // hash group-by: further hot keys in shared memory (index 2x)
     int groups = 0, aggs = 0;           // grouped plans
     std::vector<DataType> out_cols;     // table outputs: column types
     int out_dim = 0;

@@ -120,6 +120,10 @@ struct rf_table {
     long long null_count = 0;
     std::string name;
     std::vector<long long> ndv;       // cached distinct-count estimates per column (-1: unknown)
+    // hash group-by: the hottest keys of column 0, from a sample, most frequent first
+    bool hot_ready = false;
+    std::vector<long long> hot;
+    std::mutex stats_mu;              // guards ndv and hot (runs on several streams may share a table)
 };
 
 struct rf_plan {
@@ -151,6 +155,10 @@ struct rf_plan {
     void* hg_acc = nullptr;
     size_t hg_keys_cap = 0, hg_acc_cap = 0;
     long long hg_retry_cap = 0;
+    void* hg_img = nullptr;           // hot-key image of the last input table (device)
+    size_t hg_img_cap = 0;
+    const rf_table* hg_img_for = nullptr;
+    bool hg_img_some = false;         // the image holds at least one key
     // segmented reduce
     long long* seg_woff = nullptr;
     long long* seg_tmp = nullptr;

@@ -851,6 +851,7 @@ extern "C" int rf_plan_free(rf_plan* p)
     cudaFree(p->seg_woff);
     cudaFree(p->seg_tmp);
     cudaFree(p->seg_part);
+    cudaFree(p->hg_img);
     cudaFreeHost(p->h_res);
     for (auto* t : p->staging)
         if (t) {
@@ -1022,8 +1023,103 @@ namespace rfrt {
 
 // Distinct values of an int64 column, estimated with HyperLogLog (kernels.cu) and cached on the
 // table (a table statistic, as a database keeps one; computed once per uploaded table).
+// The most frequent keys of a flat int64 column 0, from a sample of up to 2^18 rows, most
+// frequent first (keys seen at least twice when every row is sampled, else three times).
+// Cached in the table.
+int hot_keys(rf_table* t, cudaStream_t s)
+{
+    std::lock_guard<std::mutex> g(t->stats_mu);
+    if (t->hot_ready) return RF_OK;
+    rf_ctx* ctx = t->ctx;
+    DevCol& dc = t->cols[0];
+    const long long n = dc.nvals, m = std::min<long long>(n, 1LL << 18);
+    std::vector<long long> h((size_t)std::max<long long>(m, 0));
+    if (m > 0) {
+        long long* d = nullptr;
+        CUDA_TRY(ctx, cudaMallocAsync((void**)&d, (size_t)m * 8, s));
+        int e = rf_k_sample_keys(dc.data, dc.valid, n, m, d, s);
+        cudaError_t ce = (cudaError_t)e;
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h.data(), d, (size_t)m * 8, cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(d, s);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+        if (ce != cudaSuccess) return fail(ctx, RF_ERR_CUDA, "key sample: %s", cudaGetErrorString(ce));
+        ctx->launches += 1;
+    }
+    std::sort(h.begin(), h.end());
+    const long long minc = m == n ? 2 : 3;
+    std::vector<std::pair<long long, long long>> cnt;  // (count, key)
+    for (size_t i = 0; i < h.size();) {
+        size_t j = i;
+        while (j < h.size() && h[j] == h[i]) j++;
+        if (h[i] != RF_EMPTY_KEY && (long long)(j - i) >= minc) cnt.push_back({(long long)(j - i), h[i]});
+        i = j;
+    }
+    std::sort(cnt.begin(), cnt.end(), [](const std::pair<long long, long long>& a, const std::pair<long long, long long>& b) {
+        return a.first != b.first ? a.first > b.first : a.second < b.second;
+    });
+    if (cnt.size() > 8192) cnt.resize(8192);
+    t->hot.clear();
+    for (auto& c : cnt) t->hot.push_back(c.second);
+    t->hot_ready = true;
+    return RF_OK;
+}
+
+// The hot-key image a hash group-by plan's aggregation kernel copies into shared memory: an
+// open-addressing index (capacity 2HK, a power of two; linear probing; the kernel's 32-bit
+// multiplicative hash of the folded key) of the HK hottest keys with ids 0..HK-1, laid out
+//   hk[2HK] i64 | hid[2HK] i32.
+// Only which rows take which path depends on it, never a result.  Null: no hot keys.
+static inline unsigned host_h32(long long key, int bits)
+{
+    const unsigned f = (unsigned)key ^ (unsigned)((unsigned long long)key >> 32);
+    return (f * 0x9E3779B1u) >> (32 - bits);
+}
+
+int hot_image(rf_plan* p, rf_table* vt, cudaStream_t s, void** img)
+{
+    *img = nullptr;
+    const int HK = p->plan.hg_hot;
+    if (HK == 0) return RF_OK;
+    int rc = hot_keys(vt, s);
+    if (rc) return rc;
+    if (p->hg_img_for == vt) {
+        *img = p->hg_img_some ? p->hg_img : nullptr;
+        return RF_OK;
+    }
+    std::vector<long long> keys;
+    {
+        std::lock_guard<std::mutex> g(vt->stats_mu);
+        keys = vt->hot;
+    }
+    p->hg_img_for = vt;
+    p->hg_img_some = !keys.empty();
+    if (keys.empty()) return RF_OK;
+    const size_t HKS = 2 * (size_t)HK, bytes = HKS * 12;
+    int bits = 0;
+    while (((size_t)1 << bits) < HKS) bits++;
+    std::vector<unsigned char> buf(bytes, 0);
+    long long* hk = (long long*)buf.data();
+    int* hid = (int*)(buf.data() + HKS * 8);
+    std::fill(hk, hk + HKS, RF_EMPTY_KEY);
+    for (size_t i = 0; i < keys.size() && (int)i < HK; i++) {
+        size_t h = host_h32(keys[i], bits);
+        while (hk[h] != RF_EMPTY_KEY) h = (h + 1) & (HKS - 1);
+        hk[h] = keys[i];
+        hid[h] = (int)i;
+    }
+    if (!grow(&p->hg_img, &p->hg_img_cap, bytes, s)) {
+        p->hg_img_for = nullptr;
+        return fail(p->ctx, RF_ERR_OOM, "hot-key image");
+    }
+    CUDA_TRY(p->ctx, cudaMemcpyAsync(p->hg_img, buf.data(), bytes, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(p->ctx, cudaStreamSynchronize(s));  // buf is released on return
+    *img = p->hg_img;
+    return RF_OK;
+}
+
 int ndv_estimate(rf_table* t, int col, cudaStream_t s, long long* out)
 {
+    std::lock_guard<std::mutex> g(t->stats_mu);
     rf_ctx* ctx = t->ctx;
     if ((int)t->ndv.size() <= col) t->ndv.resize(col + 1, -1);
     if (t->ndv[col] >= 0) {
@@ -1089,6 +1185,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         P.aux4 = p->hg_keys;
         P.aux_n0 = vt->cols[0].logical;
         P.aux_n1 = hg_cap;
+        if ((rc = hot_image(p, vt, s, &P.aux5))) return rc;
         lo = 0;
         hi = hg_cap + 1;
         P.row_lo = lo;
