@@ -131,16 +131,47 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
     }
     const long long tr = P.tile_rows;
     const long long ntiles = (P.row_hi - P.row_lo + tr - 1) / tr;
+#ifdef RF_COMPACT
+    // per-warp queue (64 rows) behind the slots: rows passing the cheap prefix of the condition
+    long long* q = (long long*)(S + (size_t)Q * T) + (size_t)warp * 64;
+#endif
     for (long long tile = unit; tile < ntiles; tile += nunits) {
         long long r0 = P.row_lo + tile * tr, r1 = r0 + tr;
         if (r1 > hi) r1 = hi;
         if (r0 < lo) r0 = lo;
+#ifdef RF_COMPACT
+        int qn = 0;
+        for (long long b = r0 + 32 * warp; b < r1; b += T) {  // warp-uniform: 32 rows per step
+            const long long r = b + lane;
+            const bool c = r < r1 && rf_cheap(P, r);
+            const unsigned m = __ballot_sync(0xffffffffu, c);
+            if (c) q[qn + __popc(m & ((1u << lane) - 1u))] = r;
+            qn += __popc(m);
+            __syncwarp();
+            if (qn >= 32) {
+                RfVals V;
+                const int g = rf_group(P, q[lane], V);
+                if (g >= 0) rf_slot_add(S, g, tid, V);
+                __syncwarp();
+                if (lane < qn - 32) q[lane] = q[32 + lane];
+                __syncwarp();
+                qn -= 32;
+            }
+        }
+        if (lane < qn) {
+            RfVals V;
+            const int g = rf_group(P, q[lane], V);
+            if (g >= 0) rf_slot_add(S, g, tid, V);
+        }
+        __syncwarp();
+#else
 #pragma unroll 4
         for (long long r = r0 + tid; r < r1; r += T) {
             RfVals V;
             int g = rf_group(P, r, V);
             if (g >= 0) rf_slot_add(S, g, tid, V);
         }
+#endif
     }
     __syncthreads();
     unsigned long long* part = (unsigned long long*)P.partials;

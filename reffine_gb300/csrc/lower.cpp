@@ -815,7 +815,36 @@ private:
     }
 
     // Get(...(state)...) chains become leaf symbols; Get(New)/Get(Select) are simplified
+    // does e (through the symbol table) reach the reduce's state?  Memoised per node: simplify
+    // asks it of every node it visits, and the accumulator expressions share subtrees.  The
+    // cache holds each node, so no address is reused while it is cached.
+    std::map<std::pair<const ExprNode*, const ExprNode*>, std::pair<Expr, bool>> mentions_memo_;
+
+    bool mentions_red(const Expr& e, const Reduce& red)
+    {
+        auto k = std::make_pair(e.get(), (const ExprNode*)red.state.get());
+        auto it = mentions_memo_.find(k);
+        if (it != mentions_memo_.end()) return it->second.second;
+        bool v = mentions(e, red.state.get(), fn_->tbl);
+        mentions_memo_.emplace(k, std::make_pair(e, v));
+        return v;
+    }
+
+    std::map<std::pair<const ExprNode*, const ExprNode*>, std::pair<Expr, Expr>> simplify_memo_;
+
+    // simplify, memoised per node (the accumulator expressions share subtrees); the cache
+    // holds each node so no address is reused while cached
     Expr simplify(const Expr& e, const Reduce& red)
+    {
+        auto k = std::make_pair(e.get(), (const ExprNode*)red.state.get());
+        auto it = simplify_memo_.find(k);
+        if (it != simplify_memo_.end()) return it->second.second;
+        Expr r = simplify_node(e, red);
+        simplify_memo_.emplace(k, std::make_pair(e, r));
+        return r;
+    }
+
+    Expr simplify_node(const Expr& e, const Reduce& red)
     {
         if (e.get() == red.state.get()) {
             if (red.state->type.is_struct()) return e;
@@ -840,7 +869,7 @@ private:
                 }
                 if (v->kind == NodeKind::SYM && v->type.is_struct()) {
                     auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(v));
-                    if (it != fn_->tbl.end() && mentions(it->second, red.state.get(), fn_->tbl))
+                    if (it != fn_->tbl.end() && mentions_red(it->second, red))
                         return simplify(std::make_shared<Get>(it->second, g->col), red);
                 }
                 if (v.get() == g->val.get()) return e;
@@ -848,29 +877,29 @@ private:
             }
             case NodeKind::SELECT: {
                 auto s = as<Select>(e);
-                if (!mentions(e, red.state.get(), fn_->tbl)) return e;
+                if (!mentions_red(e, red)) return e;
                 return std::make_shared<Select>(simplify(s->cond, red), simplify(s->true_body, red),
                                                 simplify(s->false_body, red));
             }
             case NodeKind::NARY: {
                 auto n = as<NaryExpr>(e);
-                if (!mentions(e, red.state.get(), fn_->tbl)) return e;
+                if (!mentions_red(e, red)) return e;
                 std::vector<Expr> args;
                 for (auto& a : n->args) args.push_back(simplify(a, red));
                 return std::make_shared<NaryExpr>(n->type, n->op, args);
             }
             case NodeKind::NEW: {
-                if (!mentions(e, red.state.get(), fn_->tbl)) return e;
+                if (!mentions_red(e, red)) return e;
                 std::vector<Expr> v;
                 for (auto& x : as<New>(e)->vals) v.push_back(simplify(x, red));
                 return std::make_shared<New>(v);
             }
             case NodeKind::CAST: {
-                if (!mentions(e, red.state.get(), fn_->tbl)) return e;
+                if (!mentions_red(e, red)) return e;
                 return std::make_shared<Cast>(e->type, simplify(as<Cast>(e)->arg, red));
             }
             case NodeKind::SYM: {
-                if (e->type.is_struct() || !mentions(e, red.state.get(), fn_->tbl)) return e;
+                if (e->type.is_struct() || !mentions_red(e, red)) return e;
                 auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(e));
                 if (it != fn_->tbl.end()) return simplify(it->second, red);
                 return e;
@@ -1382,6 +1411,31 @@ private:
     }
 
     // cost-ordered conjunction: cheap column predicates first, hash probes last
+    // evaluation cost class of a condition: 1 per node, 20 per element or data read, 100 per
+    // index probe (Locate)
+    int cost_of(const Expr& x)
+    {
+        std::set<const ExprNode*> seen;
+        return cost_rec(x, seen);
+    }
+
+    int cost_rec(const Expr& e, std::set<const ExprNode*>& seen)
+    {
+        if (!e || seen.count(e.get())) return 0;
+        seen.insert(e.get());
+        int k = e->kind == NodeKind::LOCATE ? 100 : e->kind == NodeKind::READDATA ? 20 : 1;
+        if (e->kind == NodeKind::SYM) {
+            auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(e));
+            if (it != fn_->tbl.end()) return cost_rec(it->second, seen);
+            return 0;
+        }
+        if (e->kind == NodeKind::ELEMENT) k = 20;
+        std::vector<Expr> ch;
+        children(e, ch);
+        for (auto& x : ch) k += cost_rec(x, seen);
+        return k;
+    }
+
     Expr order_conjuncts(const Expr& c)
     {
         std::vector<Expr> cj;
@@ -1651,6 +1705,43 @@ private:
         for (auto& dcl : dcls) o << "    " << dcl << "\n";
         o << "    if (!(" << rowcond << ")) return -1;\n";
         o << gbody << "}\n\n";
+        // Rows reach an index probe (Locate) only through cheaper filter conjuncts: the kernel
+        // then tests those first and queues the passing rows per warp, so each round of probes
+        // runs on 32 rows at once rather than on the few lanes of a warp that passed
+        // (RF_COMPACT in the template; rf_cheap is the cheap prefix of the condition).
+        bool compact = false;
+        {
+            std::string fn_text = body.str() + hoisted + gbody;
+            for (auto& dcl : dcls) fn_text += dcl;
+            std::vector<Expr> cheap;
+            if (!filters.empty() && fn_text.find("rf_locate") != std::string::npos) {
+                Expr f = filters[0];
+                for (size_t i = 1; i < filters.size(); i++) f = reffiner::_and(f, filters[i]);
+                std::vector<Expr> cj;
+                flatten_and(order_conjuncts(f), cj);
+                for (auto& c : cj) {
+                    if (cost_of(c) >= 20) break;
+                    cheap.push_back(c);
+                }
+            }
+            if (!cheap.empty()) {
+                compact = true;
+                Emitter Ec(*this);
+                std::ostringstream cbody;
+                std::string crow = bind_row(Ec, red, d, cbody);
+                Expr cf = cheap[0];
+                for (size_t i = 1; i < cheap.size(); i++) cf = reffiner::_and(cf, cheap[i]);
+                std::string cc = Ec.ev(cf).c;
+                std::vector<std::string> cd(Ec.decls.begin(), Ec.decls.end());
+                std::string cret = "    return " + cc + ";\n";
+                std::vector<std::string*> cp{&crow, &cret};
+                for (auto& x : cd) cp.push_back(&x);
+                std::string ch = hoist_row_loads(crow + cc, cp);
+                o << "RF_DEV bool rf_cheap(const RfParams& P, long long r)\n{\n" << cbody.str() << ch;
+                for (auto& x : cd) o << "    " << x << "\n";
+                o << "    if (!(" << crow << ")) return false;\n" << cret << "}\n\n#define RF_COMPACT 1\n\n";
+            }
+        }
 
         // epilogue
         Emitter Ef(*this);
@@ -1680,7 +1771,7 @@ private:
         src << o.str();
         src << "#define RF_GROUP_REDUCE 1\n#include \"rf_templates.cuh\"\n";
         src << "RF_GROUP_REDUCE_KERNEL(rf_main, " << T << ")\n";
-        size_t smem = (size_t)G * M * T * 8;
+        size_t smem = (size_t)G * M * T * 8 + (compact ? (size_t)(T / 32) * 64 * 8 : 0);
         if (smem > 200 * 1024) throw LowerError("too many group accumulators for shared memory");
         plan_.kernels.push_back({"rf_main", T, smem, KernelSpec::MAIN});
         plan_.acc_bytes = (size_t)G * M * 8;

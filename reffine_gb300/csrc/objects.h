@@ -132,6 +132,7 @@ struct rf_plan {
     rfg::Plan plan;
     std::shared_ptr<JitModule> mod;
     std::vector<CUfunction> fns;
+    void* buf = nullptr;              // the allocation holding partials .. d_res below
     void* partials = nullptr;
     size_t partials_bytes = 0;
     unsigned* counter = nullptr;

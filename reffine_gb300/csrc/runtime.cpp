@@ -790,17 +790,29 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
         p->batch_smem = mk.smem;
         p->batch_threads = mk.threads;
     }
+    // the plan's own device buffers, carved from one allocation of the context's stream-ordered
+    // pool (compiling many plans costs no device-wide synchronisation):
+    //   [partials of the units][completion counter 64 B][loop range 64 B][value result]
+    //   [table outputs: column pointer array][results 64 B]
     p->partials_bytes = (size_t)p->max_units * (p->plan.acc_bytes ? p->plan.acc_bytes : 8);
-    CUDA_TRY(ctx, cudaMalloc(&p->partials, p->partials_bytes));
-    CUDA_TRY(ctx, cudaMalloc((void**)&p->counter, 64));
-    CUDA_TRY(ctx, cudaMemset(p->counter, 0, 64));
-    CUDA_TRY(ctx, cudaMalloc((void**)&p->range, 64));
-    size_t osz = p->plan.out_size ? p->plan.out_size : 8;
-    CUDA_TRY(ctx, cudaMalloc((void**)&p->dout, (osz + 15) / 16 * 16));
+    const size_t osz = p->plan.out_size ? p->plan.out_size : 8;
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t o_counter = al(p->partials_bytes), o_range = o_counter + 256, o_out = o_range + 256;
+    const size_t o_ptrs = o_out + al(osz), o_res = o_ptrs + al(sizeof(void*) * 2 * RF_MAX_COLS);
+    const size_t total = p->plan.out_is_table ? o_res + 256 : o_ptrs;
+    unsigned char* base = nullptr;
+    CUDA_TRY(ctx, cudaMallocAsync((void**)&base, total, ctx->stream));
+    p->buf = base;
+    p->partials = base;
+    p->counter = (unsigned*)(base + o_counter);
+    p->range = (long long*)(base + o_range);
+    p->dout = base + o_out;
     if (p->plan.out_is_table) {
-        CUDA_TRY(ctx, cudaMalloc((void**)&p->d_ptrs, sizeof(void*) * 2 * RF_MAX_COLS));
-        CUDA_TRY(ctx, cudaMalloc((void**)&p->d_res, 64));
+        p->d_ptrs = (void**)(base + o_ptrs);
+        p->d_res = (long long*)(base + o_res);
     }
+    CUDA_TRY(ctx, cudaMemsetAsync(p->counter, 0, 64, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // ready for use on any stream
     *out = p.release();
     return RF_OK;
 }
@@ -839,13 +851,8 @@ extern "C" int rf_plan_free(rf_plan* p)
     if (!p) return RF_OK;
     cudaSetDevice(p->ctx->device);
     cudaStreamSynchronize(p->ctx->stream);
-    cudaFree(p->partials);
-    cudaFree(p->counter);
-    cudaFree(p->range);
-    cudaFree(p->dout);
-    cudaFree(p->d_ptrs);
+    if (p->buf) cudaFreeAsync(p->buf, p->ctx->stream);
     cudaFree(p->d_tiles);
-    cudaFree(p->d_res);
     cudaFree(p->hg_keys);
     cudaFree(p->hg_acc);
     cudaFree(p->seg_woff);
