@@ -33,53 +33,67 @@ typedef unsigned long long uint64_t;
 #define RF_DEV static __device__ __forceinline__
 
 // ---------------------------------------------------------------------------------------
-// column loads: read-only path (ld.global.nc), values are read once per query
+// column loads.  rf_ld reads a column at the scanned row: each value is read once by a query,
+// so the load is marked streaming (evict first), and a scan does not push out of L2 the data
+// that is read again - index slots and columns read at a located row (rf_rd), which keep the
+// normal read-only path.
 // ---------------------------------------------------------------------------------------
 template <class T>
 struct RfLd;
 template <>
 struct RfLd<bool> {
-    RF_DEV bool ld(const void* p, long long i) { return __ldg((const signed char*)p + i) != 0; }
+    RF_DEV bool ld(const void* p, long long i) { return __ldcs((const signed char*)p + i) != 0; }
+    RF_DEV bool ldg(const void* p, long long i) { return __ldg((const signed char*)p + i) != 0; }
 };
 template <>
 struct RfLd<int8_t> {
-    RF_DEV int8_t ld(const void* p, long long i) { return __ldg((const signed char*)p + i); }
+    RF_DEV int8_t ld(const void* p, long long i) { return __ldcs((const signed char*)p + i); }
+    RF_DEV int8_t ldg(const void* p, long long i) { return __ldg((const signed char*)p + i); }
 };
 template <>
 struct RfLd<uint8_t> {
-    RF_DEV uint8_t ld(const void* p, long long i) { return __ldg((const unsigned char*)p + i); }
+    RF_DEV uint8_t ld(const void* p, long long i) { return __ldcs((const unsigned char*)p + i); }
+    RF_DEV uint8_t ldg(const void* p, long long i) { return __ldg((const unsigned char*)p + i); }
 };
 template <>
 struct RfLd<int16_t> {
-    RF_DEV int16_t ld(const void* p, long long i) { return __ldg((const short*)p + i); }
+    RF_DEV int16_t ld(const void* p, long long i) { return __ldcs((const short*)p + i); }
+    RF_DEV int16_t ldg(const void* p, long long i) { return __ldg((const short*)p + i); }
 };
 template <>
 struct RfLd<uint16_t> {
-    RF_DEV uint16_t ld(const void* p, long long i) { return __ldg((const unsigned short*)p + i); }
+    RF_DEV uint16_t ld(const void* p, long long i) { return __ldcs((const unsigned short*)p + i); }
+    RF_DEV uint16_t ldg(const void* p, long long i) { return __ldg((const unsigned short*)p + i); }
 };
 template <>
 struct RfLd<int32_t> {
-    RF_DEV int32_t ld(const void* p, long long i) { return __ldg((const int*)p + i); }
+    RF_DEV int32_t ld(const void* p, long long i) { return __ldcs((const int*)p + i); }
+    RF_DEV int32_t ldg(const void* p, long long i) { return __ldg((const int*)p + i); }
 };
 template <>
 struct RfLd<uint32_t> {
-    RF_DEV uint32_t ld(const void* p, long long i) { return __ldg((const unsigned int*)p + i); }
+    RF_DEV uint32_t ld(const void* p, long long i) { return __ldcs((const unsigned int*)p + i); }
+    RF_DEV uint32_t ldg(const void* p, long long i) { return __ldg((const unsigned int*)p + i); }
 };
 template <>
 struct RfLd<int64_t> {
-    RF_DEV int64_t ld(const void* p, long long i) { return __ldg((const long long*)p + i); }
+    RF_DEV int64_t ld(const void* p, long long i) { return __ldcs((const long long*)p + i); }
+    RF_DEV int64_t ldg(const void* p, long long i) { return __ldg((const long long*)p + i); }
 };
 template <>
 struct RfLd<uint64_t> {
-    RF_DEV uint64_t ld(const void* p, long long i) { return __ldg((const unsigned long long*)p + i); }
+    RF_DEV uint64_t ld(const void* p, long long i) { return __ldcs((const unsigned long long*)p + i); }
+    RF_DEV uint64_t ldg(const void* p, long long i) { return __ldg((const unsigned long long*)p + i); }
 };
 template <>
 struct RfLd<float> {
-    RF_DEV float ld(const void* p, long long i) { return __ldg((const float*)p + i); }
+    RF_DEV float ld(const void* p, long long i) { return __ldcs((const float*)p + i); }
+    RF_DEV float ldg(const void* p, long long i) { return __ldg((const float*)p + i); }
 };
 template <>
 struct RfLd<double> {
-    RF_DEV double ld(const void* p, long long i) { return __ldg((const double*)p + i); }
+    RF_DEV double ld(const void* p, long long i) { return __ldcs((const double*)p + i); }
+    RF_DEV double ldg(const void* p, long long i) { return __ldg((const double*)p + i); }
 };
 
 template <class T>
@@ -88,11 +102,11 @@ RF_DEV T rf_ld(const void* p, long long i)
     return RfLd<T>::ld(p, i);
 }
 
-// guarded read of column `c` at row/run `i`
+// guarded read of column `c` at row/run `i` (a located or computed position: cached path)
 template <class T>
 RF_DEV T rf_rd(const RfCol& c, long long i)
 {
-    return (i >= 0 && i < c.len) ? rf_ld<T>(c.data, i) : T(0);
+    return (i >= 0 && i < c.len) ? RfLd<T>::ldg(c.data, i) : T(0);
 }
 
 RF_DEV bool rf_valid(const unsigned short* bm, long long i)

@@ -140,22 +140,31 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         if (r1 > hi) r1 = hi;
         if (r0 < lo) r0 = lo;
 #ifdef RF_COMPACT
+        // warp-uniform steps of 8 chunks of 32 rows: the cheap tests of all 8 are issued together
+        constexpr int U = 8;
         int qn = 0;
-        for (long long b = r0 + 32 * warp; b < r1; b += T) {  // warp-uniform: 32 rows per step
-            const long long r = b + lane;
-            const bool c = r < r1 && rf_cheap(P, r);
-            const unsigned m = __ballot_sync(0xffffffffu, c);
-            if (c) q[qn + __popc(m & ((1u << lane) - 1u))] = r;
-            qn += __popc(m);
-            __syncwarp();
-            if (qn >= 32) {
-                RfVals V;
-                const int g = rf_group(P, q[lane], V);
-                if (g >= 0) rf_slot_add(S, g, tid, V);
+        for (long long b = r0 + 32 * U * warp; b < r1; b += (long long)T * U) {
+            bool c[U];
+#pragma unroll
+            for (int j = 0; j < U; j++) {
+                const long long r = b + 32 * j + lane;
+                c[j] = r < r1 && rf_cheap(P, r);
+            }
+#pragma unroll
+            for (int j = 0; j < U; j++) {
+                const unsigned m = __ballot_sync(0xffffffffu, c[j]);
+                if (c[j]) q[qn + __popc(m & ((1u << lane) - 1u))] = b + 32 * j + lane;
+                qn += __popc(m);
                 __syncwarp();
-                if (lane < qn - 32) q[lane] = q[32 + lane];
-                __syncwarp();
-                qn -= 32;
+                if (qn >= 32) {
+                    RfVals V;
+                    const int g = rf_group(P, q[lane], V);
+                    if (g >= 0) rf_slot_add(S, g, tid, V);
+                    __syncwarp();
+                    if (lane < qn - 32) q[lane] = q[32 + lane];
+                    __syncwarp();
+                    qn -= 32;
+                }
             }
         }
         if (lane < qn) {

@@ -12,7 +12,7 @@
 
 namespace {
 
-__global__ void index_init_kernel(long long* slots, unsigned long long cap, long long* special)
+__global__ void index_init_kernel(long long* slots, unsigned long long cap, long long* special, int* dup)
 {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
@@ -22,13 +22,16 @@ __global__ void index_init_kernel(long long* slots, unsigned long long cap, long
         v.y = RF_INT64_MAX;
         reinterpret_cast<longlong2*>(slots)[i] = v;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *special = RF_INT64_MAX;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *special = RF_INT64_MAX;
+        if (dup) *dup = 0;
+    }
 }
 
 // keys: int64 column 0 (run values for a run-end column), n entries, validity bitmap or NULL
 __global__ void index_build_kernel(const long long* __restrict__ keys, const unsigned short* __restrict__ valid,
                                    long long n, long long* slots, unsigned long long cap, long long* special,
-                                   int* err)
+                                   int* err, int* dup)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     long long stride = (long long)gridDim.x * blockDim.x;
@@ -36,7 +39,7 @@ __global__ void index_build_kernel(const long long* __restrict__ keys, const uns
         if (!rf_valid(valid, i)) continue;
         long long k = __ldg(keys + i);
         if (k == RF_EMPTY_KEY) {
-            atomicMin(special, i);
+            if (atomicMin(special, i) != RF_INT64_MAX && dup) *dup = 1;
             continue;
         }
         unsigned long long h = rf_home(k, cap);
@@ -49,6 +52,7 @@ __global__ void index_build_kernel(const long long* __restrict__ keys, const uns
             if (old == (unsigned long long)RF_EMPTY_KEY)
                 old = atomicCAS(kp, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)k);
             if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)k) {
+                if (old == (unsigned long long)k && dup) *dup = 1;  // a repeated key
                 if (__ldcg(slots + 2 * h + 1) > i) atomicMin(slots + 2 * h + 1, i);
                 done = true;
                 break;
@@ -70,12 +74,12 @@ int grid_for(long long n, int threads)
 }  // namespace
 
 extern "C" int rf_k_index_build(const void* keys, const unsigned short* valid, long long n, long long* slots,
-                                unsigned long long cap, long long* special, int* err, cudaStream_t stream)
+                                unsigned long long cap, long long* special, int* err, int* dup, cudaStream_t stream)
 {
-    index_init_kernel<<<grid_for((long long)cap, 256), 256, 0, stream>>>(slots, cap, special);
+    index_init_kernel<<<grid_for((long long)cap, 256), 256, 0, stream>>>(slots, cap, special, dup);
     if (n > 0)
         index_build_kernel<<<grid_for(n, 256), 256, 0, stream>>>(static_cast<const long long*>(keys), valid, n, slots,
-                                                                 cap, special, err);
+                                                                 cap, special, err, dup);
     return (int)cudaGetLastError();
 }
 

@@ -7,9 +7,10 @@
 extern "C" {
 #endif
 
-// Builds the device hash index of an int64 key column (2 launches).  Returns a cudaError_t.
+// Builds the device hash index of an int64 key column (2 launches); *dup (if not NULL) ends 1
+// when a key occurs more than once.  Returns a cudaError_t.
 int rf_k_index_build(const void* keys, const unsigned short* valid, long long n, long long* slots,
-                     unsigned long long cap, long long* special, int* err, cudaStream_t stream);
+                     unsigned long long cap, long long* special, int* err, int* dup, cudaStream_t stream);
 
 // Exclusive prefix sum of n int64 values in place (3 launches); data must hold n+1 entries, the
 // last receives the total.  tmp must hold ceil(n / 2048) + 1 entries.

@@ -1592,6 +1592,206 @@ private:
         plan_.acc_bytes = std::max<size_t>(8, act.size() * 8);
     }
 
+    // --------------------------------------------------------------- index filter pushdown
+    // A filter conjunct that depends only on the row an index probe found - data of the probed
+    // table read at the Locate, constants, scalar inputs - can be evaluated when the index is
+    // built: a run builds a smaller index holding only the entries whose row passes, so the
+    // probes touch a table that may fit in L2.  The conjunct stays in the row filter, so a run
+    // on the full index (a batched run, rf_plan_run_noalloc) gives the same result.
+    bool ixf_analyze(const Expr& e, std::vector<Expr>& locs, std::set<const ExprNode*>& seen)
+    {
+        if (!e || seen.count(e.get())) return true;
+        seen.insert(e.get());
+        switch (e->kind) {
+            case NodeKind::CONST: return true;
+            case NodeKind::LOCATE: locs.push_back(e); return true;
+            case NodeKind::READDATA: {
+                Expr idx = as<ReadData>(e)->idx;
+                while (idx->kind == NodeKind::SYM) {
+                    auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(idx));
+                    if (it == fn_->tbl.end()) return false;
+                    idx = it->second;
+                }
+                if (idx->kind != NodeKind::LOCATE) return false;
+                if (!same(as<ReadData>(e)->vec, as<Locate>(idx)->vec)) return false;
+                locs.push_back(idx);
+                return true;
+            }
+            case NodeKind::SYM: {
+                auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(e));
+                if (it != fn_->tbl.end()) return ixf_analyze(it->second, locs, seen);
+                for (auto& in : fn_->inputs)
+                    if (in.get() == e.get()) return e->type.is_primitive();  // a scalar argument
+                return false;
+            }
+            case NodeKind::NARY: case NodeKind::SELECT: case NodeKind::CAST: {
+                std::vector<Expr> ch;
+                children(e, ch);
+                for (auto& c : ch)
+                    if (!ixf_analyze(c, locs, seen)) return false;
+                return true;
+            }
+            default: return false;
+        }
+    }
+
+    void all_locates(const Expr& e, std::vector<Expr>& out, std::set<const ExprNode*>& seen)
+    {
+        if (!e || seen.count(e.get())) return;
+        seen.insert(e.get());
+        if (e->kind == NodeKind::LOCATE) out.push_back(e);
+        if (e->kind == NodeKind::SYM) {
+            auto it = fn_->tbl.find(std::static_pointer_cast<SymNode>(e));
+            if (it != fn_->tbl.end()) all_locates(it->second, out, seen);
+            return;
+        }
+        std::vector<Expr> ch;
+        children(e, ch);
+        for (auto& c : ch) all_locates(c, out, seen);
+    }
+
+    void push_index_filter(std::ostringstream& o, const Reduce& red, const std::vector<Expr>& filters)
+    {
+        if (filters.empty()) return;
+        Expr f = filters[0];
+        for (size_t i = 1; i < filters.size(); i++) f = reffiner::_and(f, filters[i]);
+        std::vector<Expr> cj;
+        flatten_and(f, cj);
+        Expr L;
+        std::vector<Expr> pushed, locs;
+        for (auto& c : cj) {
+            std::vector<Expr> l;
+            std::set<const ExprNode*> seen;
+            if (!ixf_analyze(c, l, seen) || l.empty()) continue;
+            bool one = true;
+            for (auto& x : l) one = one && same(x, L ? L : l[0]);
+            if (!one) continue;
+            if (!L) L = l[0];
+            pushed.push_back(c);
+            locs.insert(locs.end(), l.begin(), l.end());
+        }
+        if (!L) return;
+        // the probed table must be an input with no other probe into it in the plan
+        Expr vec = as<Locate>(L)->vec;
+        int input = -1;
+        for (size_t i = 0; i < fn_->inputs.size(); i++)
+            if (fn_->inputs[i].get() == vec.get()) input = (int)i;
+        if (input < 0) return;
+        std::vector<Expr> every;
+        std::set<const ExprNode*> seen;
+        all_locates(red.acc_expr, every, seen);
+        for (auto& x : filters) all_locates(x, every, seen);
+        for (auto& x : every)
+            if (same(as<Locate>(x)->vec, vec) && !same(x, L)) return;
+        Emitter Ek(*this);
+        bind_inputs(Ek);
+        for (auto& x : locs) Ek.node_bind[x.get()] = Ek.scalar("row", types::IDX_T);
+        Expr pf = pushed[0];
+        for (size_t i = 1; i < pushed.size(); i++) pf = reffiner::_and(pf, pushed[i]);
+        std::string kc = Ek.ev(pf).c;
+        const std::string S = std::to_string(plan_.table_slot[input]);
+        o << "// the probed table's index entries whose row passes the pushed-down filter\n";
+        o << "RF_DEV bool rf_ixf_keep(const RfParams& P, long long row)\n{\n";
+        for (auto& dcl : Ek.decls) o << "    " << dcl << "\n";
+        o << "    return " << kc << ";\n}\n\n";
+        o << "#define RF_IXF_SLOT " << S << "\n";
+        o << R"(// Entries to index, 4 per thread per step.  aux_n1 == 0: the slots of the table's full index
+// (each key with the row the full index returns for it); aux_n1 == 1: the table's rows (when no
+// key repeats, the same entries, from the smaller table).  The empty key's row comes from the
+// full index's special slot in the first mode and from its row in the second.
+RF_DEV bool rf_ixf_entry(const RfParams& P, unsigned long long i, long long& key, long long& row)
+{
+    const RfIndex& ix = P.t[RF_IXF_SLOT].ix;
+    if (P.aux_n1 == 0) {
+        if (i >= ix.cap) return false;
+        const longlong2 v = __ldg((const longlong2*)ix.slots + i);
+        key = v.x;
+        row = v.y;
+        return v.x != RF_EMPTY_KEY;
+    }
+    const RfCol& c = P.t[RF_IXF_SLOT].col[0];
+    if ((long long)i >= c.len || !rf_valid(c.valid, (long long)i)) return false;
+    key = __ldcs((const long long*)c.data + i);
+    row = (long long)i;
+    return key != RF_EMPTY_KEY;
+}
+
+RF_DEV unsigned long long rf_ixf_n(const RfParams& P)
+{
+    return P.aux_n1 == 0 ? P.t[RF_IXF_SLOT].ix.cap : (unsigned long long)P.t[RF_IXF_SLOT].col[0].len;
+}
+
+// the empty key's row (the full index keeps its first row in both modes)
+RF_DEV long long rf_ixf_special(const RfParams& P) { return *P.t[RF_IXF_SLOT].ix.special; }
+
+// count of the entries to keep (aux2)
+extern "C" __global__ void __launch_bounds__(256) rf_ixf_count(const __grid_constant__ RfParams P)
+{
+    const unsigned long long n = rf_ixf_n(P), stride = gridDim.x * 256ull * 4;
+    unsigned long long c = 0;
+    for (unsigned long long b = blockIdx.x * 256ull * 4 + threadIdx.x; b < n; b += stride) {
+        long long k[4], r[4];
+        bool ok[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) ok[j] = rf_ixf_entry(P, b + j * 256ull, k[j], r[j]);
+#pragma unroll
+        for (int j = 0; j < 4; j++) c += ok[j] && rf_ixf_keep(P, r[j]);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const long long r = rf_ixf_special(P);
+        if (r != RF_INT64_MAX && rf_ixf_keep(P, r)) c++;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd((unsigned long long*)P.aux2, c);
+}
+
+// the filtered index: aux_n0 slots at aux0, its empty-key row at aux1
+extern "C" __global__ void __launch_bounds__(256) rf_ixf_init(const __grid_constant__ RfParams P)
+{
+    longlong2* t = (longlong2*)P.aux0;
+    for (long long i = blockIdx.x * 256ll + threadIdx.x; i < P.aux_n0; i += gridDim.x * 256ll) t[i] = make_longlong2(RF_EMPTY_KEY, 0);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *(long long*)P.aux1 = RF_INT64_MAX;
+}
+
+extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_constant__ RfParams P)
+{
+    longlong2* t = (longlong2*)P.aux0;
+    const unsigned long long C = (unsigned long long)P.aux_n0;
+    const unsigned long long n = rf_ixf_n(P), stride = gridDim.x * 256ull * 4;
+    for (unsigned long long b = blockIdx.x * 256ull * 4 + threadIdx.x; b < n; b += stride) {
+        long long k[4], r[4];
+        bool ok[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) ok[j] = rf_ixf_entry(P, b + j * 256ull, k[j], r[j]);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (!ok[j] || !rf_ixf_keep(P, r[j])) continue;
+            unsigned long long h = rf_home(k[j], C), m = 0;
+            for (; m < C; ++m) {
+                if (atomicCAS((unsigned long long*)&t[h].x, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)k[j]) ==
+                    (unsigned long long)RF_EMPTY_KEY) {
+                    t[h].y = r[j];
+                    break;
+                }
+                if (++h == C) h = 0;
+            }
+            if (m == C) rf_set_err(P, RF_DEVERR_OVERFLOW);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const long long r = rf_ixf_special(P);
+        if (r != RF_INT64_MAX && rf_ixf_keep(P, r)) *(long long*)P.aux1 = r;
+    }
+}
+
+)";
+        plan_.ixf_input = input;
+        plan_.kernels.push_back({"rf_ixf_count", 256, 0, KernelSpec::IXCOUNT});
+        plan_.kernels.push_back({"rf_ixf_init", 256, 0, KernelSpec::IXINIT});
+        plan_.kernels.push_back({"rf_ixf_build", 256, 0, KernelSpec::IXBUILD});
+    }
+
     void gen_group_reduce(std::ostringstream& src, const Reduce& red, const Drive& d, std::vector<Leaf>& leaves,
                           const std::vector<std::vector<int>>& groups, const std::vector<Expr>& key_exprs,
                           const std::vector<Expr>& filters)
@@ -1742,6 +1942,8 @@ private:
                 o << "    if (!(" << crow << ")) return false;\n" << cret << "}\n\n#define RF_COMPACT 1\n\n";
             }
         }
+
+        push_index_filter(o, red, filters);
 
         // epilogue
         Emitter Ef(*this);

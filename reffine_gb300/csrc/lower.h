@@ -53,7 +53,8 @@ struct KernelSpec {
     std::string name;
     int threads = 256;
     size_t smem = 0;
-    enum Role { MAIN, RANGE, STOP, COUNT, SCAN, SCATTER, INIT, FINAL, SEGCOUNT, SEGSCAN, SEGREDUCE } role = MAIN;
+    enum Role { MAIN, RANGE, STOP, COUNT, SCAN, SCATTER, INIT, FINAL, SEGCOUNT, SEGSCAN, SEGREDUCE, IXCOUNT, IXINIT,
+                IXBUILD } role = MAIN;
 };
 
 struct Plan {
@@ -80,6 +81,7 @@ struct Plan {
     bool out_is_table = false;
     size_t acc_bytes = 0;               // bytes of one unit's partial (scan-reduce, segmented reduce)
     int seg_chunk = 256;                // segmented reduce: rows per chunk
+    int ixf_input = -1;                 // input whose index a run replaces by a filtered one (-1: none)
     int hg_hot = 0;                     // hash group-by: hottest keys folded per warp (index 2x)
     int hg_warm = 0;                    // hash group-by: further hot keys in shared memory (index 2x)
     int groups = 0, aggs = 0;           // grouped plans

@@ -108,14 +108,22 @@ struct DevCol {
     size_t data_cap = 0, valid_cap = 0, re_cap = 0;
 };
 
+inline unsigned long long next_table_gen()
+{
+    static std::atomic<unsigned long long> g{0};
+    return ++g;
+}
+
 struct rf_table {
     rf_ctx* ctx = nullptr;
+    unsigned long long gen = next_table_gen();  // unique per table object, for caches keyed on tables
     long long dim = 1;
     std::vector<DevCol> cols;
     std::vector<char> present;        // column uploaded
     long long* ix_slots = nullptr;
     unsigned long long ix_cap = 0;
-    long long* ix_special = nullptr;
+    long long* ix_special = nullptr;  // [empty-key row][repeated-key flag (int)]
+    int ix_unique = -1;               // 1: no key repeats (read once from the flag), -1: unknown
     bool has_index = false;
     long long null_count = 0;
     std::string name;
@@ -158,8 +166,13 @@ struct rf_plan {
     long long hg_retry_cap = 0;
     void* hg_img = nullptr;           // hot-key image of the last input table (device)
     size_t hg_img_cap = 0;
-    const rf_table* hg_img_for = nullptr;
+    unsigned long long hg_img_for = 0;  // generation of the table the image was built for
     bool hg_img_some = false;         // the image holds at least one key
+    // filtered index of a probed table (plans with a pushed-down filter)
+    void* ixf_buf = nullptr;
+    size_t ixf_cap = 0;
+    unsigned long long ixf_for = 0;   // generation of the table whose kept-entry count is ixf_count
+    long long ixf_count = 0;
     // segmented reduce
     long long* seg_woff = nullptr;
     long long* seg_tmp = nullptr;

@@ -426,11 +426,14 @@ int upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int6
         t = owned.get();
     }
     t->ctx = ctx;
+    t->gen = next_table_gen();  // new contents: caches keyed on the table start over
     t->dim = dim;
     t->name = schema->name ? schema->name : "";
     t->has_index = false;
     t->null_count = 0;
     t->ndv.assign(n, -1);
+    t->hot_ready = false;
+    t->hot.clear();
     t->cols.resize(n);
     t->present.assign(n, 0);
     std::vector<char> want(n, sel ? 0 : 1);
@@ -499,6 +502,7 @@ int upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int6
 int build_index(rf_table* t, cudaStream_t s)
 {
     rf_ctx* ctx = t->ctx;
+    t->gen = next_table_gen();
     if (t->cols.empty()) return fail(ctx, RF_ERR_INVALID, "empty table");
     DevCol& c0 = t->cols[0];
     if (c0.type.btype != reffine::INT64)
@@ -511,9 +515,12 @@ int build_index(rf_table* t, cudaStream_t s)
     t->ix_slots = nullptr;
     t->ix_special = nullptr;
     if (cudaMallocAsync((void**)&t->ix_slots, cap * 16, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
-    if (cudaMallocAsync((void**)&t->ix_special, 8, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
+    // [empty-key row, 8 B][repeated-key flag, 4 B]
+    if (cudaMallocAsync((void**)&t->ix_special, 16, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
     t->ix_cap = cap;
-    int e = rf_k_index_build(c0.data, c0.valid, c0.nvals, t->ix_slots, cap, t->ix_special, ctx->dev_err, s);
+    t->ix_unique = -1;
+    int e = rf_k_index_build(c0.data, c0.valid, c0.nvals, t->ix_slots, cap, t->ix_special, ctx->dev_err,
+                             (int*)(t->ix_special + 1), s);
     if (e) return fail(ctx, RF_ERR_CUDA, "index build launch failed: %s", cudaGetErrorString((cudaError_t)e));
     ctx->launches += c0.nvals > 0 ? 2 : 1;
     t->has_index = true;
@@ -859,6 +866,7 @@ extern "C" int rf_plan_free(rf_plan* p)
     cudaFree(p->seg_tmp);
     cudaFree(p->seg_part);
     cudaFree(p->hg_img);
+    cudaFree(p->ixf_buf);
     cudaFreeHost(p->h_res);
     for (auto* t : p->staging)
         if (t) {
@@ -974,6 +982,65 @@ int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long lo
     return RF_OK;
 }
 
+bool index_role(int role)
+{
+    return role == rfg::KernelSpec::IXCOUNT || role == rfg::KernelSpec::IXINIT || role == rfg::KernelSpec::IXBUILD;
+}
+
+// Builds the plan's filtered index of the probed table T (its index entries whose row passes
+// the pushed-down filter, see the lowering) on stream s and points `out` at it.  The number of
+// entries kept is counted once per table (a synchronising read) and remembered.
+int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, RfIndex* out)
+{
+    rf_ctx* ctx = p->ctx;
+    const rfg::Plan& pl = p->plan;
+    CUfunction fc = nullptr, fi = nullptr, fb = nullptr;
+    for (size_t i = 0; i < pl.kernels.size(); i++) {
+        if (pl.kernels[i].role == rfg::KernelSpec::IXCOUNT) fc = p->fns[i];
+        if (pl.kernels[i].role == rfg::KernelSpec::IXINIT) fi = p->fns[i];
+        if (pl.kernels[i].role == rfg::KernelSpec::IXBUILD) fb = p->fns[i];
+    }
+    // without repeated keys the entries come from the table's rows (smaller than its index)
+    if (T->ix_unique < 0) {
+        int dup = 0;
+        CUDA_TRY(ctx, cudaMemcpyAsync(&dup, T->ix_special + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        T->ix_unique = dup ? 0 : 1;
+    }
+    const long long mode = T->ix_unique == 1 ? 1 : 0;
+    const unsigned long long nent = mode ? (unsigned long long)T->cols[0].nvals : T->ix_cap;
+    const int gfull = (int)std::min<unsigned long long>((nent + 1023) / 1024 + 1, (unsigned long long)ctx->sm_count * 8);
+    int rc;
+    if (p->ixf_for != T->gen) {
+        if (!grow(&p->ixf_buf, &p->ixf_cap, 256, s)) return fail(ctx, RF_ERR_OOM, "filtered index");
+        CUDA_TRY(ctx, cudaMemsetAsync(p->ixf_buf, 0, 8, s));
+        RfParams Q = P;
+        Q.aux2 = p->ixf_buf;
+        Q.aux_n1 = mode;
+        if ((rc = launch(ctx, fc, gfull, 256, 0, s, &Q))) return rc;
+        unsigned long long n = 0;
+        CUDA_TRY(ctx, cudaMemcpyAsync(&n, p->ixf_buf, 8, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        p->ixf_count = (long long)n;
+        p->ixf_for = T->gen;
+    }
+    unsigned long long cap = 64;
+    while (cap < 2 * (unsigned long long)p->ixf_count) cap *= 2;
+    if (!grow(&p->ixf_buf, &p->ixf_cap, cap * 16 + 256, s)) return fail(ctx, RF_ERR_OOM, "filtered index");
+    RfParams Q = P;
+    Q.aux0 = p->ixf_buf;
+    Q.aux_n0 = (long long)cap;
+    Q.aux1 = (unsigned char*)p->ixf_buf + cap * 16;
+    Q.aux_n1 = mode;
+    const int gcap = (int)std::min<unsigned long long>((cap + 255) / 256, (unsigned long long)ctx->sm_count * 8);
+    if ((rc = launch(ctx, fi, gcap, 256, 0, s, &Q))) return rc;
+    if ((rc = launch(ctx, fb, gfull, 256, 0, s, &Q))) return rc;
+    out->slots = (const long long*)p->ixf_buf;
+    out->cap = cap;
+    out->special = (const long long*)Q.aux1;
+    return RF_OK;
+}
+
 int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams* Pout)
 {
     rf_ctx* ctx = p->ctx;
@@ -985,8 +1052,13 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
     long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
     int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
     P.nunits = units;
+    if (pl.ixf_input >= 0) {
+        RfTab& tab = P.t[pl.table_slot[pl.ixf_input]];
+        if ((rc = filtered_index(p, args[pl.ixf_input].table, P, s, &tab.ix))) return rc;
+    }
     for (size_t i = 0; i < pl.kernels.size(); i++) {
         const auto& k = pl.kernels[i];
+        if (index_role(k.role)) continue;
         int grid = 1;
         switch (k.role) {
             case rfg::KernelSpec::RANGE: grid = 1; break;
@@ -1089,7 +1161,7 @@ int hot_image(rf_plan* p, rf_table* vt, cudaStream_t s, void** img)
     if (HK == 0) return RF_OK;
     int rc = hot_keys(vt, s);
     if (rc) return rc;
-    if (p->hg_img_for == vt) {
+    if (p->hg_img_for == vt->gen) {
         *img = p->hg_img_some ? p->hg_img : nullptr;
         return RF_OK;
     }
@@ -1098,7 +1170,7 @@ int hot_image(rf_plan* p, rf_table* vt, cudaStream_t s, void** img)
         std::lock_guard<std::mutex> g(vt->stats_mu);
         keys = vt->hot;
     }
-    p->hg_img_for = vt;
+    p->hg_img_for = vt->gen;
     p->hg_img_some = !keys.empty();
     if (keys.empty()) return RF_OK;
     const size_t HKS = 2 * (size_t)HK, bytes = HKS * 12;
@@ -1115,7 +1187,7 @@ int hot_image(rf_plan* p, rf_table* vt, cudaStream_t s, void** img)
         hid[h] = (int)i;
     }
     if (!grow(&p->hg_img, &p->hg_img_cap, bytes, s)) {
-        p->hg_img_for = nullptr;
+        p->hg_img_for = 0;
         return fail(p->ctx, RF_ERR_OOM, "hot-key image");
     }
     CUDA_TRY(p->ctx, cudaMemcpyAsync(p->hg_img, buf.data(), bytes, cudaMemcpyHostToDevice, s));
@@ -1397,6 +1469,7 @@ extern "C" int rf_plan_run_noalloc(rf_plan* p, const rf_arg* args, int32_t n_arg
     CUDA_TRY(ctx, cudaMemsetAsync(P.counter, 0, sizeof(unsigned int), s));
     for (size_t i = 0; i < pl.kernels.size(); i++) {
         const auto& k = pl.kernels[i];
+        if (index_role(k.role)) continue;  // runs on the full index: same result, no allocation
         int grid = k.role == rfg::KernelSpec::RANGE ? 1
                    : k.role == rfg::KernelSpec::STOP
                        ? (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8)

@@ -69,6 +69,26 @@ def test_join_group_counts(eng, groups):
     assert_same(got, loopgen.Query(fn)(b, p))
 
 
+@pytest.mark.parametrize("dups", [False, True])
+def test_join_filtered_index_matches_full_probe(eng, dups):
+    # the build-side filter (attr < 5) is applied while the probed index is built; with
+    # repeated build keys the filtered index must keep exactly the row the full index returns
+    # (the first), whatever the other rows of the key hold
+    rng = np.random.default_rng(21)
+    nb, npr = 50_000, 600_011
+    keys = rng.integers(0, 20_000, nb).astype(np.int64) if dups else rng.permutation(1 << 20)[:nb].astype(np.int64)
+    build = Table.from_arrays(1, {"key": keys, "attr": rng.integers(0, 25, nb, dtype=np.int32)}, name="build")
+    fk = keys[rng.integers(0, nb, npr)]
+    probe = Table.from_arrays(2, {"row": np.arange(npr, dtype=np.int64), "fk": fk,
+                                  "amount": rng.uniform(1.0, 10000.0, npr), "day": rng.integers(0, 2557, npr, dtype=np.int32)})
+    fn = W.join_query(build.get_data_type(), probe.get_data_type(), 5, 0, 900)
+    plan = eng.compile(fn)
+    db, dp = eng.upload(build).build_index(), eng.upload(probe)
+    got = plan.run(db, dp)
+    assert_same(got, loopgen.Query(fn)(build, probe))
+    assert got == plan.run(db, dp)  # the second run reuses the kept-entry count
+
+
 def test_validity_of_column_one_gates_rows(eng):
     # loopgen.cpp:238: a SubVector reduce skips rows whose column-1 value is null
     t = W.filter_sum_table(100_000, seed=3)
