@@ -263,7 +263,7 @@ def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5)
     tab = [i for i, r in enumerate(wl.requests) if r.plan.info.output_is_table]
     sample = set(tab[:: max(1, len(tab) // 40)])  # ~40 table results compared in full, all by row count
     alone = serve.run_alone(eng, wl.requests, sample)
-    keep = ("qps", "gbps", "p50_us", "p99_us", "mean_us", "mean_batch", "failed", "mismatches")
+    keep = ("qps", "gbps", "p50_us", "p99_us", "mean_us", "mean_batch", "failed", "mismatches", "failures")
     slim = lambda d: {k: (round(d[k], 3) if isinstance(d[k], float) else d[k]) for k in keep}
     out = {"queries": len(wl.requests),
            "shapes": dict(zip(serve.SHAPES, np.bincount([r.shape for r in wl.requests], minlength=4).tolist())),

@@ -168,9 +168,7 @@ struct rf_plan {
     size_t hg_img_cap = 0;
     unsigned long long hg_img_for = 0;  // generation of the table the image was built for
     bool hg_img_some = false;         // the image holds at least one key
-    // filtered index of a probed table (plans with a pushed-down filter)
-    void* ixf_buf = nullptr;
-    size_t ixf_cap = 0;
+    // filtered index of a probed table (plans with a pushed-down filter): its entry count
     unsigned long long ixf_for = 0;   // generation of the table whose kept-entry count is ixf_count
     long long ixf_count = 0;
     // segmented reduce

@@ -866,7 +866,6 @@ extern "C" int rf_plan_free(rf_plan* p)
     cudaFree(p->seg_tmp);
     cudaFree(p->seg_part);
     cudaFree(p->hg_img);
-    cudaFree(p->ixf_buf);
     cudaFreeHost(p->h_res);
     for (auto* t : p->staging)
         if (t) {
@@ -988,19 +987,21 @@ bool index_role(int role)
 }
 
 // Builds the plan's filtered index of the probed table T (its index entries whose row passes
-// the pushed-down filter, see the lowering) on stream s and points `out` at it.  The number of
-// entries kept is counted once per table (a synchronising read) and remembered.
-int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, RfIndex* out)
+// the pushed-down filter, see the lowering) on stream s, in memory taken from the stream-ordered
+// pool for this run (*buf; the caller releases it after the probing kernel), and points `out`
+// at it.  The number of entries kept is counted once per table (a synchronising read) and
+// remembered; the entries come from T's rows when no key repeats, else from its index.
+int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, RfIndex* out, void** buf)
 {
     rf_ctx* ctx = p->ctx;
     const rfg::Plan& pl = p->plan;
+    *buf = nullptr;
     CUfunction fc = nullptr, fi = nullptr, fb = nullptr;
     for (size_t i = 0; i < pl.kernels.size(); i++) {
         if (pl.kernels[i].role == rfg::KernelSpec::IXCOUNT) fc = p->fns[i];
         if (pl.kernels[i].role == rfg::KernelSpec::IXINIT) fi = p->fns[i];
         if (pl.kernels[i].role == rfg::KernelSpec::IXBUILD) fb = p->fns[i];
     }
-    // without repeated keys the entries come from the table's rows (smaller than its index)
     if (T->ix_unique < 0) {
         int dup = 0;
         CUDA_TRY(ctx, cudaMemcpyAsync(&dup, T->ix_special + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1012,30 +1013,37 @@ int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, R
     const int gfull = (int)std::min<unsigned long long>((nent + 1023) / 1024 + 1, (unsigned long long)ctx->sm_count * 8);
     int rc;
     if (p->ixf_for != T->gen) {
-        if (!grow(&p->ixf_buf, &p->ixf_cap, 256, s)) return fail(ctx, RF_ERR_OOM, "filtered index");
-        CUDA_TRY(ctx, cudaMemsetAsync(p->ixf_buf, 0, 8, s));
+        unsigned long long* cnt = nullptr;
+        CUDA_TRY(ctx, cudaMallocAsync((void**)&cnt, 8, s));
+        CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, 8, s));
         RfParams Q = P;
-        Q.aux2 = p->ixf_buf;
+        Q.aux2 = cnt;
         Q.aux_n1 = mode;
-        if ((rc = launch(ctx, fc, gfull, 256, 0, s, &Q))) return rc;
+        rc = launch(ctx, fc, gfull, 256, 0, s, &Q);
         unsigned long long n = 0;
-        CUDA_TRY(ctx, cudaMemcpyAsync(&n, p->ixf_buf, 8, cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        cudaError_t e = rc ? cudaSuccess : cudaMemcpyAsync(&n, cnt, 8, cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(cnt, s);
+        if (rc) return rc;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail(ctx, RF_ERR_CUDA, "filtered index count: %s", cudaGetErrorString(e));
         p->ixf_count = (long long)n;
         p->ixf_for = T->gen;
     }
     unsigned long long cap = 64;
     while (cap < 2 * (unsigned long long)p->ixf_count) cap *= 2;
-    if (!grow(&p->ixf_buf, &p->ixf_cap, cap * 16 + 256, s)) return fail(ctx, RF_ERR_OOM, "filtered index");
+    if (cudaMallocAsync(buf, cap * 16 + 256, s) != cudaSuccess) {
+        *buf = nullptr;
+        return fail(ctx, RF_ERR_OOM, "filtered index (%llu slots)", cap);
+    }
     RfParams Q = P;
-    Q.aux0 = p->ixf_buf;
+    Q.aux0 = *buf;
     Q.aux_n0 = (long long)cap;
-    Q.aux1 = (unsigned char*)p->ixf_buf + cap * 16;
+    Q.aux1 = (unsigned char*)*buf + cap * 16;
     Q.aux_n1 = mode;
     const int gcap = (int)std::min<unsigned long long>((cap + 255) / 256, (unsigned long long)ctx->sm_count * 8);
     if ((rc = launch(ctx, fi, gcap, 256, 0, s, &Q))) return rc;
     if ((rc = launch(ctx, fb, gfull, 256, 0, s, &Q))) return rc;
-    out->slots = (const long long*)p->ixf_buf;
+    out->slots = (const long long*)*buf;
     out->cap = cap;
     out->special = (const long long*)Q.aux1;
     return RF_OK;
@@ -1052,11 +1060,15 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
     long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
     int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
     P.nunits = units;
+    void* ixbuf = nullptr;
     if (pl.ixf_input >= 0) {
         RfTab& tab = P.t[pl.table_slot[pl.ixf_input]];
-        if ((rc = filtered_index(p, args[pl.ixf_input].table, P, s, &tab.ix))) return rc;
+        if ((rc = filtered_index(p, args[pl.ixf_input].table, P, s, &tab.ix, &ixbuf))) {
+            if (ixbuf) cudaFreeAsync(ixbuf, s);
+            return rc;
+        }
     }
-    for (size_t i = 0; i < pl.kernels.size(); i++) {
+    for (size_t i = 0; i < pl.kernels.size() && !rc; i++) {
         const auto& k = pl.kernels[i];
         if (index_role(k.role)) continue;
         int grid = 1;
@@ -1067,8 +1079,10 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
             case rfg::KernelSpec::MAIN: grid = units; break;
             default: grid = units; break;
         }
-        if ((rc = launch(ctx, p->fns[i], grid, k.threads, k.smem, s, &P))) return rc;
+        rc = launch(ctx, p->fns[i], grid, k.threads, k.smem, s, &P);
     }
+    if (ixbuf) cudaFreeAsync(ixbuf, s);  // after the kernels that read it, in stream order
+    if (rc) return rc;
     if (Pout) *Pout = P;
     return RF_OK;
 }
