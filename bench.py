@@ -272,7 +272,8 @@ def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5)
            "bytes_per_query_mb": round(sum(r.nbytes for r in wl.requests) / len(wl.requests) / 1e6, 2),
            "server": "2 lanes x 256 queries per launch, 8 GiB scratch budget", "workload_build_s": round(t_build, 1),
            "check": "value results bit for bit; table results by row count, %d of them key-sorted in full "
-                    "(FP64 within 1e-12)" % len(sample)}
+                    "(FP64 within 1e-12)" % len(sample),
+           "tile_rows_tuned": wl.tuning}
     closed = {}
     for mode in ("per_query", "batched"):
         closed[mode] = slim(serve.serve_run(eng, wl, mode, math.inf, alone, check_tables=True))

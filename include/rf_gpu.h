@@ -22,6 +22,7 @@
  *                                   a host function pointer with the generated function's signature
  *   rf_batch_*                      no counterpart: batching of many queries into one persistent launch
  *   rf_server_*                     no counterpart: continuous-batching request loop
+ *   rf_plan_tune, rf_tune_*         no counterpart: tiling autotuner
  *   rf_last_error                   no counterpart: the reference exits or aborts on errors
  *                                   (src/engine/cuda_engine.cpp:10-23)
  */
@@ -175,6 +176,15 @@ int rf_batch_wait(rf_batch* b);
  * by rf_batch_wait), 0 while it runs. */
 int rf_batch_poll(rf_batch* b, int32_t* done);
 int rf_batch_reset(rf_batch* b);
+
+/* ---- autotuner (no reference counterpart) --------------------------------------------------
+ * Times the tiling of a Reduce scan (rows per unit of work, 1K..32K) on the given inputs and
+ * records the fastest for the plan's query shape and the input's log2 row-count bucket; every
+ * later run of that shape and bucket in this context (alone, batched, served) uses it.  The
+ * table of choices is exported and imported as text lines "shape-key bucket tile-rows". */
+int rf_plan_tune(rf_plan* plan, const rf_arg* args, int32_t n_args, int32_t reps, int64_t* tile_rows, double* ms);
+int rf_tune_export(rf_ctx* ctx, char* buf, size_t len, size_t* needed);
+int rf_tune_import(rf_ctx* ctx, const char* text);
 
 /* ---- serving: continuous batching over resident tables (no reference counterpart) ---------
  * A server owns a scheduler thread.  Batched mode packs the pending Reduce queries into

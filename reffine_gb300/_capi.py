@@ -90,6 +90,9 @@ SIGNATURES = {
     "rf_batch_reset": (I, [P]),
     "rf_batch_poll": (I, [P, ctypes.POINTER(I32)]),
     "rf_clock_ns": (I64, []),
+    "rf_plan_tune": (I, [P, ctypes.POINTER(RfArg), I32, I32, ctypes.POINTER(I64), ctypes.POINTER(ctypes.c_double)]),
+    "rf_tune_export": (I, [P, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "rf_tune_import": (I, [P, ctypes.c_char_p]),
     "rf_server_create": (I, [P, ctypes.POINTER(RfServerConfig), PP]),
     "rf_server_submit": (I, [P, P, ctypes.POINTER(RfArg), I32, P, ctypes.c_uint64]),
     "rf_server_cancel": (I, [P, ctypes.c_uint64]),

@@ -167,7 +167,7 @@ extern "C" int rf_batch_add(rf_batch* b, rf_plan* plan, const rf_arg* args, int3
     long long lo, hi;
     int rc = fill_params(plan, args, n_args, it.P, lo, hi, true);
     if (rc) return rc;
-    long long ntiles = (hi - lo + plan->plan.tile_rows - 1) / plan->plan.tile_rows;
+    long long ntiles = (hi - lo + it.P.tile_rows - 1) / it.P.tile_rows;
     it.units = (int)std::min<long long>(std::max<long long>(ntiles, 1), plan->max_units);
     it.P.nunits = it.units;
     b->items.push_back(it);

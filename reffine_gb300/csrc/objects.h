@@ -90,6 +90,9 @@ struct rf_ctx {
     std::atomic<long long> launches{0};
     int sm_count = 0;
     int* dev_err = nullptr;  // device error word shared by this context's launches
+    // autotuner choices: tile rows per (query shape key, log2 row-count bucket)
+    std::mutex tune_mu;
+    std::map<std::string, std::map<int, long long>> tune;
 };
 
 struct DevCol {
@@ -148,6 +151,7 @@ struct rf_plan {
     unsigned char* dout = nullptr;
     int max_units = 0;
     int thunk_slot = -1;
+    long long tile_override = 0;      // set while the autotuner times a candidate
     unsigned char* h_res = nullptr;   // pinned: [error word, 16 B][value result]
     // batched execution (value-output plans without device-computed loop bounds)
     CUfunction batch_fn = nullptr;
@@ -201,6 +205,7 @@ int launch(rf_ctx* ctx, CUfunction f, int grid, int block, size_t smem, cudaStre
 int fail(rf_ctx* ctx, int code, const char* fmt, ...);
 int check_device_error(rf_ctx* ctx);
 int device_error(rf_ctx* ctx, int e);  // RF_OK for 0, else clears the context's error word and fails
+long long tile_rows_for(rf_plan* p, long long rows);  // the tiling a run of `rows` rows uses
 void batch_set_share(rf_batch* b, int pct);
 int cu_fail(rf_ctx* ctx, CUresult r, const char* what);
 }  // namespace rfrt

@@ -17,6 +17,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -901,6 +902,24 @@ extern "C" int rf_plan_info(rf_plan* p, rf_plan_info_t* info)
 
 namespace rfrt {
 
+// Tiling of a scan: the rows of one unit of work.  Scan and grouped-scan Reduce plans take the
+// autotuner's choice for their shape and size bucket when there is one (rf_plan_tune); every
+// path of a query (alone, batched, without allocation) asks here, so all use the same tiling and
+// give the same result bits.
+long long tile_rows_for(rf_plan* p, long long rows)
+{
+    const rfg::Plan& pl = p->plan;
+    if (pl.kind != rfg::PlanKind::SCAN_REDUCE && pl.kind != rfg::PlanKind::GROUP_REDUCE) return pl.tile_rows;
+    if (p->tile_override > 0) return p->tile_override;
+    int bucket = 0;
+    while (bucket < 62 && (1LL << (bucket + 1)) <= rows) bucket++;
+    std::lock_guard<std::mutex> g(p->ctx->tune_mu);
+    auto it = p->ctx->tune.find(pl.key);
+    if (it == p->ctx->tune.end()) return pl.tile_rows;
+    auto jt = it->second.find(bucket);
+    return jt == it->second.end() ? pl.tile_rows : jt->second;
+}
+
 int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long long& lo, long long& hi,
                 bool may_allocate)
 {
@@ -972,7 +991,7 @@ int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long lo
     if (hi < lo) hi = lo;
     P.row_lo = lo;
     P.row_hi = hi;
-    P.tile_rows = pl.tile_rows;
+    P.tile_rows = tile_rows_for(p, hi - lo);
     P.range = pl.device_range ? p->range : nullptr;
     P.partials = p->partials;
     P.counter = p->counter;
@@ -1057,7 +1076,7 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
     int rc = fill_params(p, args, n_args, P, lo, hi, true);
     if (rc) return rc;
     const rfg::Plan& pl = p->plan;
-    long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
+    long long ntiles = (hi - lo + P.tile_rows - 1) / P.tile_rows;
     int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
     P.nunits = units;
     void* ixbuf = nullptr;
@@ -1098,6 +1117,107 @@ std::vector<rf_table*>& staging_of(rf_plan* p)
     return p->staging;
 }
 }  // namespace rfrt
+
+// ------------------------------------------------------------------------------------------
+// autotuner
+// ------------------------------------------------------------------------------------------
+extern "C" int rf_plan_tune(rf_plan* p, const rf_arg* args, int32_t n_args, int32_t reps, int64_t* tile_rows,
+                            double* ms)
+{
+    if (!p) return RF_ERR_INVALID;
+    rf_ctx* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    const rfg::Plan& pl = p->plan;
+    if (pl.out_is_table || (pl.kind != rfg::PlanKind::SCAN_REDUCE && pl.kind != rfg::PlanKind::GROUP_REDUCE))
+        return fail(ctx, RF_ERR_UNSUPPORTED, "the autotuner tunes the tiling of Reduce scans");
+    if (reps < 1) reps = 3;
+    RfParams P;
+    long long lo, hi;
+    int rc = fill_params(p, args, n_args, P, lo, hi, true);
+    if (rc) return rc;
+    const long long rows = std::max<long long>(hi - lo, 1);
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(ctx, cudaEventCreate(&e0));
+    CUDA_TRY(ctx, cudaEventCreate(&e1));
+    long long best = 0;
+    float best_ms = 0;
+    // candidate tilings from 1K rows to 32K rows (no tile much larger than the input)
+    for (long long t = 1024; t <= 32768; t *= 2) {
+        if (t > 2 * rows && best) break;
+        p->tile_override = t;
+        std::vector<float> v;
+        for (int r = 0; r <= reps && !rc; r++) {
+            cudaEventRecord(e0, s);
+            rc = enqueue(p, args, n_args, s, nullptr);
+            cudaEventRecord(e1, s);
+            if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(ctx, RF_ERR_CUDA, "autotuner timing");
+            float x = 0;
+            cudaEventElapsedTime(&x, e0, e1);
+            if (r) v.push_back(x);  // the first run is a warm-up
+        }
+        if (rc) break;
+        std::sort(v.begin(), v.end());
+        const float med = v[v.size() / 2];
+        if (!best || med < best_ms) {
+            best = t;
+            best_ms = med;
+        }
+    }
+    p->tile_override = 0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = check_device_error(ctx))) return rc;
+    int bucket = 0;
+    while (bucket < 62 && (1LL << (bucket + 1)) <= rows) bucket++;
+    {
+        std::lock_guard<std::mutex> g(ctx->tune_mu);
+        ctx->tune[pl.key][bucket] = best;
+    }
+    if (tile_rows) *tile_rows = best;
+    if (ms) *ms = best_ms;
+    return RF_OK;
+}
+
+extern "C" int rf_tune_export(rf_ctx* ctx, char* buf, size_t len, size_t* needed)
+{
+    if (!ctx) return RF_ERR_INVALID;
+    std::string t;
+    {
+        std::lock_guard<std::mutex> g(ctx->tune_mu);
+        for (auto& kv : ctx->tune)
+            for (auto& b : kv.second) t += kv.first + " " + std::to_string(b.first) + " " + std::to_string(b.second) + "\n";
+    }
+    if (needed) *needed = t.size() + 1;
+    if (buf && len) {
+        size_t n = std::min(len - 1, t.size());
+        memcpy(buf, t.data(), n);
+        buf[n] = 0;
+        if (n < t.size()) return fail(ctx, RF_ERR_INVALID, "buffer of %zu bytes holds %zu of the tuning table", len, n);
+    }
+    return RF_OK;
+}
+
+extern "C" int rf_tune_import(rf_ctx* ctx, const char* text)
+{
+    if (!ctx || !text) return RF_ERR_INVALID;
+    std::istringstream in(text);
+    std::string key;
+    int bucket;
+    long long tile;
+    std::map<std::string, std::map<int, long long>> add;
+    while (in >> key >> bucket >> tile) {
+        if (bucket < 0 || bucket > 62 || tile < 32 || tile > (1LL << 30))
+            return fail(ctx, RF_ERR_INVALID, "tuning entry %s %d %lld out of range", key.c_str(), bucket, tile);
+        add[key][bucket] = tile;
+    }
+    if (!in.eof()) return fail(ctx, RF_ERR_INVALID, "malformed tuning table");
+    std::lock_guard<std::mutex> g(ctx->tune_mu);
+    for (auto& kv : add)
+        for (auto& b : kv.second) ctx->tune[kv.first][b.first] = b.second;
+    return RF_OK;
+}
 
 extern "C" int rf_plan_launch(rf_plan* p, const rf_arg* args, int32_t n_args, void* dev_out, void* stream)
 {
@@ -1329,7 +1449,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         free_table_mem(t.get());
         return rc;
     }
-    long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
+    long long ntiles = (hi - lo + P.tile_rows - 1) / P.tile_rows;
     if ((size_t)std::max<long long>(ntiles, 1) * 8 > p->tiles_cap) {  // tiles_cap: bytes
         if (!grow((void**)&p->d_tiles, &p->tiles_cap, (size_t)std::max<long long>(ntiles, 1024) * 8, s)) {
             free_table_mem(t.get());
@@ -1464,7 +1584,7 @@ extern "C" int rf_plan_run_noalloc(rf_plan* p, const rf_arg* args, int32_t n_arg
     long long lo, hi;
     int rc = fill_params(p, args, n_args, P, lo, hi, false);
     if (rc) return rc;
-    long long ntiles = (hi - lo + pl.tile_rows - 1) / pl.tile_rows;
+    long long ntiles = (hi - lo + P.tile_rows - 1) / P.tile_rows;
     int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
     // layout: [counter 256][loop bounds 256][result, 256-aligned][partials: units x acc_bytes]
     size_t out_bytes = (pl.out_size + 255) / 256 * 256;

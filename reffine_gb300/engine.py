@@ -99,6 +99,31 @@ class Engine:
         self.check(self.lib.rf_plan_compile(self.h, fn.text().encode(), int(vectorize), ctypes.byref(h)))
         return Plan(self, h, fn, vectorize)
 
+    def tune_export(self) -> str:
+        """The autotuner's choices as text lines "shape-key bucket tile-rows"."""
+        need = ctypes.c_size_t()
+        self.check(self.lib.rf_tune_export(self.h, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        self.check(self.lib.rf_tune_export(self.h, buf, need.value, None))
+        return buf.value.decode()
+
+    def tune_import(self, text: str):
+        self.check(self.lib.rf_tune_import(self.h, text.encode()))
+
+    def tune_save(self, path: str):
+        """Persists the autotuner's choices as JSON (entries keyed by query shape and size bucket)."""
+        import json
+        entries = [{"shape": k, "bucket": int(b), "tile_rows": int(t)}
+                   for k, b, t in (l.split() for l in self.tune_export().splitlines() if l.strip())]
+        with open(path, "w") as f:
+            json.dump({"version": 1, "entries": entries}, f, indent=1)
+
+    def tune_load(self, path: str):
+        import json
+        with open(path) as f:
+            d = json.load(f)
+        self.tune_import("".join("%s %d %d\n" % (e["shape"], e["bucket"], e["tile_rows"]) for e in d["entries"]))
+
     def host_alloc(self, nbytes: int) -> "PinnedBuffer":
         return PinnedBuffer(self, nbytes)
 
@@ -255,6 +280,14 @@ class Plan:
 
     def new_out(self):
         return self._out_ct()
+
+    def tune(self, *inputs, reps: int = 3):
+        """Autotunes the scan tiling for these inputs' size bucket (rf_plan_tune); returns
+        (tile_rows, ms of the fastest)."""
+        args = self.args(*inputs)
+        t, ms = ctypes.c_int64(), ctypes.c_double()
+        self.eng.check(self.eng.lib.rf_plan_tune(self.h, args, len(inputs), reps, ctypes.byref(t), ctypes.byref(ms)))
+        return t.value, ms.value
 
     def thunk(self):
         """The host query function (reference calling shape) as a ctypes function pointer."""

@@ -118,6 +118,7 @@ class Workload:
     requests: List[Request]
     tables: Dict[int, list] = field(default_factory=dict)  # shape -> [(host Table(s), DeviceTable(s))]
     resident_bytes: int = 0
+    tuning: Dict[str, int] = field(default_factory=dict)  # "shape/rows" -> tile rows chosen
 
 
 def log_uniform_sizes(rng, k: int, lo: int, hi: int) -> List[int]:
@@ -129,7 +130,8 @@ def _prefix(t: Table, n: int) -> Table:
 
 
 def build_workload(eng: Engine, n_queries: int = 10_000, tables_per_shape: int = 6, min_rows: int = 1_000,
-                   max_rows: int = 50_000_000, seed: int = 4, shapes: Sequence[int] = (0, 1, 2, 3)) -> Workload:
+                   max_rows: int = 50_000_000, seed: int = 4, shapes: Sequence[int] = (0, 1, 2, 3),
+                   tune: bool = True) -> Workload:
     """Tables per shape with log-uniform row counts in [min_rows, max_rows] (each a prefix of one
     seeded table of the largest drawn size), uploaded once; then n_queries requests, each a
     uniform shape, a uniform table of that shape and fresh filter constants."""
@@ -180,6 +182,7 @@ def build_workload(eng: Engine, n_queries: int = 10_000, tables_per_shape: int =
         return plan_cache[key]
 
     shape_list = list(wl.tables)
+    tuned = {}  # (shape, table index) -> first plan of that shape on that table
     for _ in range(n_queries):
         s = shape_list[int(rng.integers(0, len(shape_list)))]
         pool = wl.tables[s]
@@ -204,6 +207,17 @@ def build_workload(eng: Engine, n_queries: int = 10_000, tables_per_shape: int =
             req = Request(3, plan_of(fn), dev, len(p),
                           W.algorithmic_bytes(b, [0, 1]) + W.algorithmic_bytes(p, [1, 2, 3]), host)
         wl.requests.append(req)
+    if tune:
+        # the autotuner's tiling for each Reduce shape and table size (one representative query
+        # each; the choice applies to every query of the shape and size bucket)
+        for r in wl.requests:
+            if r.plan.info.output_is_table:
+                continue
+            key = (r.shape, r.rows)
+            if key in tuned:
+                continue
+            tuned[key] = r.plan.tune(*r.inputs)
+        wl.tuning = {"%s/%d" % (SHAPES[k[0]], k[1]): v[0] for k, v in sorted(tuned.items())}
     return wl
 
 

@@ -1,0 +1,50 @@
+"""The tiling autotuner: its choice is used by every later run of the query shape and size
+bucket (alone and batched alike, so the results keep the same bits), results stay within the
+oracle's tolerance, and the choices survive export/import and the JSON file."""
+import pytest
+
+from oracle import loopgen
+from parity import assert_same
+from reffine_gb300 import engine, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tune_filter_sum_and_groupby(eng, tmp_path):
+    t = W.filter_sum_table(3_000_017, seed=41)
+    dt = eng.upload(t)
+    plan = eng.compile(W.filter_sum_query(t.get_data_type(), 700, 1300))
+    before = plan.run(dt)
+    tile, ms = plan.tune(dt, reps=3)
+    assert tile in (1024, 2048, 4096, 8192, 16384, 32768) and ms > 0
+    after = plan.run(dt)
+    ref = loopgen.Query(plan.fn)(t)
+    assert_same(after, ref)
+    assert_same(before, ref)
+    # another query of the same shape (other constants) takes the same tiling; batched runs too
+    other = eng.compile(W.filter_sum_query(t.get_data_type(), 100, 2000))
+    b = engine.Batch(eng, 4)
+    o1, o2 = b.add(plan, dt), b.add(other, dt)
+    b.launch()
+    got = b.wait()
+    assert got[0] == after and got[1] == other.run(dt)
+    text = eng.tune_export()
+    assert str(tile) in text and len(text.splitlines()) >= 1
+    g = W.groupby_table(1_000_003, seed=42)
+    dg = eng.upload(g)
+    gp = eng.compile(W.groupby_query(g.get_data_type()))
+    gt, _ = gp.tune(dg)
+    assert_same(gp.run(dg), loopgen.Query(gp.fn)(g))
+    path = str(tmp_path / "tune.json")
+    eng.tune_save(path)
+    eng2 = engine.Engine()
+    eng2.tune_load(path)
+    assert sorted(eng2.tune_export().splitlines()) == sorted(eng.tune_export().splitlines())
+    eng2.close()
+
+
+def test_tune_rejects_table_outputs(eng):
+    t = W.hashgroup_table(10_000, 100, seed=43)
+    plan = eng.compile(W.hashgroup_query(t.get_data_type()))
+    with pytest.raises(RuntimeError, match="UNSUPPORTED"):
+        plan.tune(eng.upload(t))
