@@ -23,6 +23,7 @@
  *   rf_batch_*                      no counterpart: batching of many queries into one persistent launch
  *   rf_server_*                     no counterpart: continuous-batching request loop
  *   rf_plan_tune, rf_tune_*         no counterpart: tiling autotuner
+ *   rf_ipc_read, rf_table_load_ipc  load_arrow_file (src/utils/utils.cpp:11-34), without Arrow C++
  *   rf_last_error                   no counterpart: the reference exits or aborts on errors
  *                                   (src/engine/cuda_engine.cpp:10-23)
  */
@@ -118,6 +119,13 @@ int rf_table_column(rf_table* t, int32_t col, int32_t part, void** dev_ptr, int6
 int rf_table_export(rf_table* t, struct ArrowSchema* schema_out, struct ArrowArray* array_out);
 /* Null count of the table (vectorised Op outputs mark filtered rows invalid). */
 int rf_table_null_count(rf_table* t, int64_t* nulls);
+/* Arrow IPC ingest (load_arrow_file, src/utils/utils.cpp:11-34): record batch 0 of an Arrow
+ * IPC file - integer, float and run-end encoded columns, uncompressed, no dictionaries.
+ * rf_ipc_read needs no GPU: it returns the batch as Arrow C data (a "+s" struct of the
+ * columns, as ArrowTable2 holds it; release both objects to free it); on failure `err` holds
+ * the reason.  rf_table_load_ipc reads the file straight into a device table. */
+int rf_ipc_read(const char* path, struct ArrowSchema* schema, struct ArrowArray* array, char* err, size_t err_len);
+int rf_table_load_ipc(rf_ctx* ctx, const char* path, int64_t dim, void* stream, rf_table** out);
 
 /* ---- plans -------------------------------------------------------------------------------- */
 /* Lowers a Reffine Func (its text form, include/reffine_gb300/ir.h) onto a kernel template,

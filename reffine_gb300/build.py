@@ -26,7 +26,7 @@ LIB = os.path.join(LIBDIR, "librf_gpu.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-HOST_SRCS = ["lower.cpp", "runtime.cpp", "thunks.cpp", "batch.cpp", "server.cpp"]
+HOST_SRCS = ["lower.cpp", "runtime.cpp", "thunks.cpp", "batch.cpp", "server.cpp", "ipc.cpp"]
 CUDA_SRCS = ["kernels.cu"]
 EMBED = ["rf_device.cuh", "rf_templates.cuh", "rf_params.h"]
 

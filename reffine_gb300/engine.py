@@ -94,6 +94,20 @@ class Engine:
             dt.build_index()
         return dt
 
+    def load_ipc(self, path: str, dim: int) -> "DeviceTable":
+        """Record batch 0 of an Arrow IPC file, read by the library's parser and copied straight
+        to the device (the role of load_arrow_file, src/utils/utils.cpp:11-34)."""
+        from .table import ir_type_of_c, read_ipc_c, release_c
+        s, a = read_ipc_c(path)
+        try:
+            h = ctypes.c_void_p()
+            self.check(self.lib.rf_table_upload(self.h, ctypes.byref(s), ctypes.byref(a), dim, None, ctypes.byref(h)))
+            self.sync()  # the file's memory is released next
+            names = [s.children[c].contents.name.decode() for c in range(s.n_children)]
+            return DeviceTable(self, h, ir_type_of_c(s, dim), names)
+        finally:
+            release_c(s, a)
+
     def compile(self, fn: ir.Func, vectorize: bool = False) -> "Plan":
         h = ctypes.c_void_p()
         self.check(self.lib.rf_plan_compile(self.h, fn.text().encode(), int(vectorize), ctypes.byref(h)))

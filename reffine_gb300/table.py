@@ -16,6 +16,7 @@ by the Table.
 from __future__ import annotations
 
 import ctypes
+import os
 from typing import Dict, List, Optional, Sequence
 
 import numpy as np
@@ -223,3 +224,81 @@ def ree_encode(keys: np.ndarray):
     starts = np.concatenate([[0], brk])
     ends = np.concatenate([brk, [len(keys)]]).astype(np.int32)
     return keys[starts], ends
+
+
+# ---------------------------------------------------------------------------------------------
+# Arrow IPC files (load_arrow_file, src/utils/utils.cpp:11-34), read by the library's own parser
+# ---------------------------------------------------------------------------------------------
+DTYPE_OF_FMT = {"c": "i8", "s": "i16", "i": "i32", "l": "i64", "C": "u8", "S": "u16", "I": "u32", "L": "u64",
+                "f": "f32", "g": "f64"}
+
+
+def read_ipc_c(path: str):
+    """Record batch 0 of an Arrow IPC file as (ArrowSchema, ArrowArray); release_c frees them."""
+    from . import _capi
+    s, a = ArrowSchema(), ArrowArray()
+    err = ctypes.create_string_buffer(512)
+    rc = _capi.load().rf_ipc_read(path.encode(), ctypes.byref(s), ctypes.byref(a), err, len(err))
+    if rc:
+        raise _capi.RfError(rc, err.value.decode(errors="replace"))
+    return s, a
+
+
+def release_c(s: "ArrowSchema", a: "ArrowArray"):
+    if a.release:
+        ctypes.CFUNCTYPE(None, ctypes.POINTER(ArrowArray))(a.release)(ctypes.byref(a))
+    if s.release:
+        ctypes.CFUNCTYPE(None, ctypes.POINTER(ArrowSchema))(s.release)(ctypes.byref(s))
+
+
+def ir_type_of_c(s: "ArrowSchema", dim: int) -> ir.DataType:
+    """The vector type of a "+s" table schema (ArrowTable2::get_data_type, table.h:62-80)."""
+    types, encs = [], []
+    for c in range(s.n_children):
+        cs = s.children[c].contents
+        fmt = cs.format.decode()
+        if fmt == "+r":
+            types.append(ir.DataType(DTYPE_OF_FMT[cs.children[1].contents.format.decode()]))
+            encs.append(ir.RUNEND)
+        else:
+            types.append(ir.DataType(DTYPE_OF_FMT[fmt]))
+            encs.append(ir.FLAT)
+    return ir.DataType("vector", types, dim, encs)
+
+
+def _copy(ptr, n: int, dtype) -> np.ndarray:
+    out = np.zeros(n, dtype=dtype)
+    if n and ptr:
+        ctypes.memmove(out.ctypes.data, ptr, n * out.itemsize)
+    return out
+
+
+def _bitmap(ptr, n: int) -> Optional[np.ndarray]:
+    if not ptr:
+        return None
+    out = np.zeros(max(((n + 15) // 16) * 2, 2), dtype=np.uint8)
+    ctypes.memmove(out.ctypes.data, ptr, ((n + 15) // 16) * 2)
+    return out
+
+
+def table_from_ipc(path: str, dim: int, name: Optional[str] = None) -> Table:
+    """A host Table holding record batch 0 of an Arrow IPC file (copied out of the file)."""
+    s, a = read_ipc_c(path)
+    try:
+        cols = []
+        for c in range(s.n_children):
+            cs, ca = s.children[c].contents, a.children[c].contents
+            nm, fmt = cs.name.decode(), cs.format.decode()
+            if fmt == "+r":
+                re_a = ca.children[0].contents
+                vs, va = cs.children[1].contents, ca.children[1].contents
+                dt = DTYPE_OF_FMT[vs.format.decode()]
+                run_ends = _copy(re_a.buffers[1], re_a.length, np.int32)
+                cols.append(Column(nm, dt, _copy(va.buffers[1], va.length, NP_OF[dt]), _bitmap(va.buffers[0], va.length),
+                                   run_ends))
+            else:
+                dt = DTYPE_OF_FMT[fmt]
+                cols.append(Column(nm, dt, _copy(ca.buffers[1], ca.length, NP_OF[dt]), _bitmap(ca.buffers[0], ca.length)))
+        return Table(name or os.path.splitext(os.path.basename(path))[0], dim, cols)
+    finally:
+        release_c(s, a)
