@@ -9,8 +9,15 @@
 // the reference's JIT modules do.
 //
 // ArrowTable2 mirrors the reference's owning table (include/reffine/arrow/table.h:15-151):
-// (name, dim, len, column names, types) allocates flat columns; get_data_type() derives the
-// vector type (a "+r" child is run-end encoded).
+// (name, dim, len, column names, types) allocates flat columns; (dim) is an empty table that
+// adopts Arrow C data (load_arrow_file fills it); get_data_type() derives the vector type from
+// the column formats (a "+r" child is run-end encoded).
+//
+// load_arrow_file(filename, dim) (include/reffine/utils/utils.h:56, src/utils/utils.cpp:11-34)
+// reads record batch 0 of an Arrow IPC file with the library's own parser (rf_ipc_read: integer,
+// float and run-end encoded columns; compressed bodies and dictionaries are refused) and throws
+// std::runtime_error with the parser's message on failure, where the reference aborts through
+// ValueOrDie.
 #pragma once
 
 #include <cstdlib>
@@ -75,6 +82,16 @@ T compile_op(std::shared_ptr<Func> op, bool vectorize = false)
 
 // ---- an owning host table in Reffine's layout -------------------------------------------------
 struct ArrowTable2 : public ArrowTable {
+    // an empty table whose schema/array are filled by a producer of Arrow C data
+    // (table.h:16-22); the producer's release callbacks run when the table is destroyed
+    explicit ArrowTable2(int64_t dim) : ArrowTable(dim)
+    {
+        std::memset(&top_s_, 0, sizeof top_s_);
+        std::memset(&top_a_, 0, sizeof top_a_);
+        schema = &top_s_;
+        array = &top_a_;
+    }
+
     ArrowTable2(std::string name, int64_t dim, size_t len, std::vector<std::string> cols, std::vector<DataType> dtypes)
         : ArrowTable(dim), name_(std::move(name))
     {
@@ -129,17 +146,42 @@ struct ArrowTable2 : public ArrowTable {
         return reinterpret_cast<V*>(bufs_.at(c).data());
     }
 
-    // ArrowTable2::get_data_type (table.h:62-80)
+    ~ArrowTable2() override
+    {
+        if (top_a_.release) top_a_.release(&top_a_);
+        if (top_s_.release) top_s_.release(&top_s_);
+    }
+    ArrowTable2(const ArrowTable2&) = delete;
+    ArrowTable2& operator=(const ArrowTable2&) = delete;
+
+    // ArrowTable2::get_data_type (table.h:64-80): one element type per child, "+r" = run-end
     DataType get_data_type() const
     {
-        std::vector<EncodeType> enc(types_.size(), FLAT);
-        return DataType(VECTOR, types_, (size_t)dim, enc);
+        std::vector<DataType> dts;
+        std::vector<EncodeType> enc;
+        for (int64_t i = 0; i < schema->n_children; i++) {
+            const ArrowSchema* c = schema->children[i];
+            bool ree = std::strcmp(c->format, "+r") == 0;
+            dts.push_back(dtype_of(ree ? c->children[1]->format : c->format));
+            enc.push_back(ree ? RUNEND : FLAT);
+        }
+        return DataType(VECTOR, dts, (size_t)dim, enc);
     }
 
     // the GPU backend builds its own device index when a query probes this table
     void build_index() {}
 
 private:
+    // arrow_to_dtype (table.h:82-104), with the unsigned widths the IPC reader also produces
+    static DataType dtype_of(const char* f)
+    {
+        static const char* fmts = "csilCSILfg";
+        static const BaseType bts[] = {INT8, INT16, INT32, INT64, UINT8, UINT16, UINT32, UINT64, FLOAT32, FLOAT64};
+        if (f && f[0] && !f[1])
+            for (int k = 0; fmts[k]; k++)
+                if (fmts[k] == f[0]) return DataType(bts[k]);
+        throw std::runtime_error(std::string("schema type not supported ") + (f ? f : "(null)"));
+    }
     static std::string format_of(const DataType& t)
     {
         switch (t.btype) {
@@ -165,5 +207,14 @@ private:
     ArrowArray top_a_;
     const void* top_bufs_[1] = {nullptr};
 };
+
+inline std::shared_ptr<ArrowTable2> load_arrow_file(std::string filename, int64_t dim)
+{
+    auto tbl = std::make_shared<ArrowTable2>(dim);
+    char err[512];
+    if (rf_ipc_read(filename.c_str(), tbl->schema, tbl->array, err, sizeof err) != RF_OK)
+        throw std::runtime_error("load_arrow_file: " + std::string(err));
+    return tbl;
+}
 
 }  // namespace reffine
