@@ -291,6 +291,71 @@ def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5)
     return out
 
 
+def bench_ingest(eng, config: int, rows: int = 0, reps: int = 3):
+    """Arrow IPC ingest (load_arrow_file, src/utils/utils.cpp:11-34): the config's table written
+    as an IPC file (the page cache holds it after the write; disk speed is not measured), then
+    host_read: rf_ipc_read, file -> host Arrow C data (what the reference's load does, CPU only);
+    load: rf_table_load_ipc, file -> HBM, streamed through the pinned staging ring;
+    read_then_upload: rf_ipc_read, then rf_table_upload from its pageable memory.
+    The config's query runs on the loaded table and on an upload of the in-memory table: both
+    results must have the same bits."""
+    import ctypes
+    import shutil
+    import tempfile
+    from reffine_gb300.ipc_write import write_ipc
+    from reffine_gb300.table import read_ipc_c, release_c
+    name, tables, fn, nrows, cfg = build_workload(config, 0, 1, rows)
+    if len(tables) != 1:
+        raise ValueError("ingest is measured on single-table configurations (0, 1, 2)")
+    t = tables[0]
+    d = tempfile.mkdtemp(prefix="rf_ingest_")
+    try:
+        path = os.path.join(d, name + ".arrow")
+        t0 = time.perf_counter()
+        size = write_ipc(path, t)
+        t_write = time.perf_counter() - t0
+
+        def host_read():
+            s, a = read_ipc_c(path)
+            release_c(s, a)
+
+        def load():
+            eng.load_ipc(path, t.dim).free()
+            eng.sync()
+
+        def read_then_upload():
+            s, a = read_ipc_c(path)
+            try:
+                h = ctypes.c_void_p()
+                eng.check(eng.lib.rf_table_upload(eng.h, ctypes.byref(s), ctypes.byref(a), t.dim, None, ctypes.byref(h)))
+                eng.sync()
+                eng.lib.rf_table_free(h)
+            finally:
+                release_c(s, a)
+
+        res = {}
+        for nm, f in (("host_read", host_read), ("load", load), ("read_then_upload", read_then_upload)):
+            f()  # first run: allocations, staging ring, page cache settled
+            ts = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                f()
+                ts.append(time.perf_counter() - t0)
+            res[nm] = {"gbps": round(size / min(ts) / 1e9, 2), "ms_best": round(min(ts) * 1e3, 2),
+                       "ms_median": round(float(np.median(ts)) * 1e3, 2)}
+        loaded = eng.load_ipc(path, t.dim)
+        plan = eng.compile(fn)
+        same = plan.run(loaded) == plan.run(eng.upload(t))
+        loaded.free()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {"metric": "arrow_ipc_ingest", "unit": "GB/s (file bytes / wall time, best of %d)" % reps,
+            "workload": name, "rows": nrows, "file_bytes": size, "write_s": round(t_write, 2),
+            "page_cache": "warm (file just written)", "host_threads": os.cpu_count(),
+            **res, "load_vs_host_read": round(res["host_read"]["ms_best"] / res["load"]["ms_best"], 2),
+            "query_result_identical": bool(same)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -304,10 +369,18 @@ def main():
     ap.add_argument("--serving-queries", type=int, default=10_000,
                     help="requests of the batched-serving comparison (0: skip it)")
     ap.add_argument("--serving-max-rows", type=int, default=50_000_000)
+    ap.add_argument("--ingest", action="store_true",
+                    help="measure Arrow IPC ingest of the config's table instead (one JSON line)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.ingest:
+        from reffine_gb300 import engine
+        eng = engine.Engine(local)
+        print(json.dumps(bench_ingest(eng, args.config, args.rows)), flush=True)
+        eng.close()
+        return 0
 
     from reffine_gb300 import cudart, engine
     dist = Dist(world)

@@ -119,6 +119,11 @@ int rf_table_column(rf_table* t, int32_t col, int32_t part, void** dev_ptr, int6
 int rf_table_export(rf_table* t, struct ArrowSchema* schema_out, struct ArrowArray* array_out);
 /* Null count of the table (vectorised Op outputs mark filtered rows invalid). */
 int rf_table_null_count(rf_table* t, int64_t* nulls);
+/* One line per column, "name<TAB>format<TAB>flat|runend\n" (Arrow format strings: "l" int64,
+ * "g" double, ...; a run-end column gives its values' format), written to buf (NUL-terminated,
+ * truncated to len); *needed = the full text's length + 1.  The column types of
+ * ArrowTable2::get_data_type (table.h:64-80) for a table that has no host-side schema. */
+int rf_table_describe(rf_table* t, char* buf, size_t len, size_t* needed);
 /* Arrow IPC ingest (load_arrow_file, src/utils/utils.cpp:11-34): record batch 0 of an Arrow
  * IPC file - integer, float and run-end encoded columns, uncompressed, no dictionaries.
  * rf_ipc_read needs no GPU: it returns the batch as Arrow C data (a "+s" struct of the

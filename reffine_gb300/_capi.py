@@ -73,6 +73,7 @@ SIGNATURES = {
     "rf_table_column": (I, [P, I32, I32, PP, ctypes.POINTER(I64)]),
     "rf_table_export": (I, [P, ctypes.POINTER(ArrowSchema), ctypes.POINTER(ArrowArray)]),
     "rf_table_null_count": (I, [P, ctypes.POINTER(I64)]),
+    "rf_table_describe": (I, [P, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "rf_ipc_read": (I, [ctypes.c_char_p, ctypes.POINTER(ArrowSchema), ctypes.POINTER(ArrowArray), ctypes.c_char_p,
                         ctypes.c_size_t]),
     "rf_table_load_ipc": (I, [P, ctypes.c_char_p, I64, P, PP]),

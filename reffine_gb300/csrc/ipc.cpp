@@ -10,6 +10,12 @@
 // the file's size; anything outside the supported subset - compressed bodies, dictionaries,
 // types other than integers, floats and run-end encoded columns of them - is refused with a
 // message, never read.
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <cerrno>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -21,6 +27,7 @@
 #include "objects.h"
 #include "reffine_gb300/arrow_c.h"
 #include "rf_gpu.h"
+#include "runtime.h"
 
 namespace {
 
@@ -256,45 +263,14 @@ struct Reader {
     }
 };
 
-}  // namespace
-
-extern "C" int rf_ipc_read(const char* path, ArrowSchema* schema, ArrowArray* array, char* err, size_t err_len)
+// Parses record batch 0 of the IPC file image `b` into Arrow C data whose buffers point into
+// the image; `h` keeps the exported structs (and, for rf_ipc_read, the image itself).
+int parse_file(const Buf& b, Holder* h, ArrowSchema* schema, ArrowArray* array, std::string& err)
 {
-    auto put = [&](const std::string& m) {
-        if (err && err_len) {
-            size_t n = std::min(err_len - 1, m.size());
-            std::memcpy(err, m.data(), n);
-            err[n] = 0;
-        }
-    };
-    if (!path || !schema || !array) {
-        put("null argument");
-        return RF_ERR_INVALID;
-    }
     std::memset(schema, 0, sizeof *schema);
     std::memset(array, 0, sizeof *array);
-    std::unique_ptr<Holder> h(new Holder);
-    {
-        FILE* f = std::fopen(path, "rb");
-        if (!f) {
-            put(std::string("cannot open ") + path);
-            return RF_ERR_INVALID;
-        }
-        std::fseek(f, 0, SEEK_END);
-        long sz = std::ftell(f);
-        std::fseek(f, 0, SEEK_SET);
-        if (sz < 0) sz = 0;
-        h->file.resize((size_t)sz);
-        size_t got = sz ? std::fread(h->file.data(), 1, (size_t)sz, f) : 0;
-        std::fclose(f);
-        if (got != (size_t)sz) {
-            put(std::string("cannot read ") + path);
-            return RF_ERR_INVALID;
-        }
-    }
     try {
-        Reader r{Buf{h->file.data(), h->file.size()}, h.get(), 0, 0, Vec(), Vec(), 0, 0};
-        const Buf& b = r.b;
+        Reader r{b, h, 0, 0, Vec(), Vec(), 0, 0};
         // file: "ARROW1" 2 bytes of padding ... footer, int32 footer size, "ARROW1"
         if (b.n < 18 || std::memcmp(b.p, "ARROW1", 6) != 0 || std::memcmp(b.p + b.n - 6, "ARROW1", 6) != 0)
             throw IpcError{"not an Arrow IPC file (magic)"};
@@ -355,37 +331,131 @@ extern "C" int rf_ipc_read(const char* path, ArrowSchema* schema, ArrowArray* ar
         schema->n_children = (int64_t)n;
         schema->children = h->schema_kids.back().data();
         schema->release = release_top_schema;
-        schema->private_data = h.get();
+        schema->private_data = h;
         array->length = rows;
         array->n_buffers = 1;
         array->buffers = h->buffers.back().data();
         array->n_children = (int64_t)n;
         array->children = h->array_kids.back().data();
         array->release = release_top_array;
-        array->private_data = h.get();
-        h.release();
+        array->private_data = h;
         return RF_OK;
     } catch (const IpcError& e) {
-        put(e.msg);
+        err = e.msg;
         std::memset(schema, 0, sizeof *schema);
         std::memset(array, 0, sizeof *array);
         return e.msg.find("not supported") != std::string::npos ? RF_ERR_UNSUPPORTED : RF_ERR_INVALID;
     }
 }
 
+// the file's bytes [off, off + n) into dst, whole (pread returns short counts near page-cache
+// boundaries and on signals)
+bool pread_all(int fd, void* dst, size_t n, size_t off)
+{
+    char* d = (char*)dst;
+    while (n) {
+        const ssize_t got = ::pread(fd, d, n, (off_t)off);
+        if (got < 0 && errno == EINTR) continue;
+        if (got <= 0) return false;
+        d += got, off += (size_t)got, n -= (size_t)got;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" int rf_ipc_read(const char* path, ArrowSchema* schema, ArrowArray* array, char* err, size_t err_len)
+{
+    auto put = [&](const std::string& m) {
+        if (err && err_len) {
+            size_t n = std::min(err_len - 1, m.size());
+            std::memcpy(err, m.data(), n);
+            err[n] = 0;
+        }
+    };
+    if (!path || !schema || !array) {
+        put("null argument");
+        return RF_ERR_INVALID;
+    }
+    std::memset(schema, 0, sizeof *schema);
+    std::memset(array, 0, sizeof *array);
+    std::unique_ptr<Holder> h(new Holder);
+    {
+        FILE* f = std::fopen(path, "rb");
+        if (!f) {
+            put(std::string("cannot open ") + path);
+            return RF_ERR_INVALID;
+        }
+        std::fseek(f, 0, SEEK_END);
+        long sz = std::ftell(f);
+        std::fseek(f, 0, SEEK_SET);
+        if (sz < 0) sz = 0;
+        h->file.resize((size_t)sz);
+        size_t got = sz ? std::fread(h->file.data(), 1, (size_t)sz, f) : 0;
+        std::fclose(f);
+        if (got != (size_t)sz) {
+            put(std::string("cannot read ") + path);
+            return RF_ERR_INVALID;
+        }
+    }
+    std::string msg;
+    const int rc = parse_file(Buf{h->file.data(), h->file.size()}, h.get(), schema, array, msg);
+    if (rc) {
+        put(msg);
+        return rc;
+    }
+    h.release();  // owned by the two exported objects now
+    return RF_OK;
+}
+
+// The file is mapped for the parser (it touches only the footer and the message metadata) and
+// its body is streamed to the device: reader threads pread slices of the column buffers into the
+// pinned staging ring while the previous slices' DMA runs (staged_h2d).  No host copy of the
+// whole file is made.
 extern "C" int rf_table_load_ipc(rf_ctx* ctx, const char* path, int64_t dim, void* stream, rf_table** out)
 {
-    if (!ctx || !out) return RF_ERR_INVALID;
-    ArrowSchema s;
-    ArrowArray a;
-    char msg[512];
-    int rc = rf_ipc_read(path, &s, &a, msg, sizeof msg);
-    if (rc) return rfrt::fail(ctx, rc, "%s", msg);
-    rc = rf_table_upload(ctx, &s, &a, dim, stream, out);
-    // the file's memory is released next: the copies out of it must have finished
-    if (!rc && cudaStreamSynchronize(stream ? (cudaStream_t)stream : ctx->stream) != cudaSuccess)
-        rc = rfrt::fail(ctx, RF_ERR_CUDA, "table upload from %s", path);
-    a.release(&a);
-    s.release(&s);
+    if (!ctx || !out || !path) return ctx ? rfrt::fail(ctx, RF_ERR_INVALID, "null argument") : RF_ERR_INVALID;
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    const int fd = ::open(path, O_RDONLY | O_CLOEXEC);
+    if (fd < 0) return rfrt::fail(ctx, RF_ERR_INVALID, "cannot open %s", path);
+    struct stat st;
+    if (::fstat(fd, &st) != 0 || st.st_size < 18) {
+        ::close(fd);
+        return rfrt::fail(ctx, RF_ERR_INVALID, "%s: not an Arrow IPC file (too short)", path);
+    }
+    const size_t size = (size_t)st.st_size;
+    void* map = ::mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
+    if (map == MAP_FAILED) {
+        ::close(fd);
+        return rfrt::fail(ctx, RF_ERR_INVALID, "cannot map %s", path);
+    }
+    ::posix_fadvise(fd, 0, 0, POSIX_FADV_SEQUENTIAL);
+    const uint8_t* base = (const uint8_t*)map;
+    ArrowSchema sc;
+    ArrowArray ar;
+    std::string msg;
+    Holder* h = new Holder;
+    int rc = parse_file(Buf{base, size}, h, &sc, &ar, msg);
+    if (rc) {
+        delete h;
+        rc = rfrt::fail(ctx, rc, "%s", msg.c_str());
+    } else {
+        std::vector<rfrt::HostCopy> copies;
+        rc = rfrt::upload(ctx, &sc, &ar, dim, nullptr, 0, s, out, nullptr, &copies);
+        if (!rc)
+            rc = rfrt::staged_h2d(ctx, copies, [&](void* dst, const void* src, size_t n) {
+                return pread_all(fd, dst, n, (size_t)((const uint8_t*)src - base));
+            }, s);
+        if (rc && *out) {
+            rf_table_free(*out);
+            *out = nullptr;
+        }
+        ar.release(&ar);
+        sc.release(&sc);
+    }
+    ::munmap(map, size);
+    ::close(fd);
     return rc;
 }

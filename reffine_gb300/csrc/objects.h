@@ -93,6 +93,10 @@ struct rf_ctx {
     // autotuner choices: tile rows per (query shape key, log2 row-count bucket)
     std::mutex tune_mu;
     std::map<std::string, std::map<int, long long>> tune;
+    // pinned staging ring for host copies from files and pageable memory (staged_h2d)
+    std::mutex stage_mu;
+    unsigned char* stage = nullptr;
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
 };
 
 struct DevCol {

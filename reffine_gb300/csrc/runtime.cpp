@@ -19,6 +19,8 @@
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
+#include <condition_variable>
 #include <vector>
 
 #include "arrow_c.h"
@@ -281,6 +283,9 @@ extern "C" int rf_gpu_shutdown(rf_ctx* ctx)
     cudaStreamSynchronize(ctx->stream);
     ctx->modules.clear();
     cudaFree(ctx->dev_err);
+    if (ctx->stage) cudaFreeHost(ctx->stage);
+    for (auto& e : ctx->stage_ev)
+        if (e) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return RF_OK;
@@ -365,7 +370,8 @@ namespace {
 
 // copies `bytes` from host `src` into the allocation (*buf, *cap), growing it if needed;
 // *active is set to the copy, or NULL when there is nothing to copy
-int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src, size_t bytes, cudaStream_t s)
+int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src, size_t bytes, cudaStream_t s,
+            std::vector<HostCopy>* defer)
 {
     *active = nullptr;
     if (!src || bytes == 0) return RF_OK;
@@ -378,10 +384,127 @@ int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src
             return fail(ctx, RF_ERR_OOM, "cudaMallocAsync(%zu) failed", bytes);
         *cap = bytes;
     }
-    CUDA_TRY(ctx, cudaMemcpyAsync(*buf, src, bytes, cudaMemcpyHostToDevice, s));
+    if (defer)
+        defer->push_back({*buf, src, bytes});
+    else
+        CUDA_TRY(ctx, cudaMemcpyAsync(*buf, src, bytes, cudaMemcpyHostToDevice, s));
     *active = *buf;
     return RF_OK;
 }
+
+// Pinned staging ring: two halves of kStageSlots slots of kStageChunk bytes (128 MiB in all),
+// allocated on first use and kept by the context.
+constexpr size_t kStageChunk = size_t(4) << 20;
+constexpr size_t kStageSlots = 16;
+
+}  // namespace
+
+namespace rfrt {
+
+int staged_h2d(rf_ctx* ctx, const std::vector<HostCopy>& copies,
+               const std::function<bool(void*, const void*, size_t)>& fill, cudaStream_t s)
+{
+    struct Piece {
+        void* dst;
+        const void* src;
+        size_t n;
+    };
+    std::vector<Piece> pieces;
+    for (const HostCopy& c : copies)
+        for (size_t o = 0; o < c.bytes; o += kStageChunk)
+            pieces.push_back({(char*)c.dst + o, (const char*)c.src + o, std::min(kStageChunk, c.bytes - o)});
+    if (pieces.empty()) return RF_OK;
+    std::lock_guard<std::mutex> g(ctx->stage_mu);
+    if (!ctx->stage) {
+        CUDA_TRY(ctx, cudaHostAlloc((void**)&ctx->stage, 2 * kStageSlots * kStageChunk, cudaHostAllocDefault));
+        for (auto& e : ctx->stage_ev) CUDA_TRY(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    // fillers: every thread takes slots of the current round until none is left
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nthreads = std::min({hw, size_t(16), pieces.size()});
+    std::mutex m;
+    std::condition_variable cv_work, cv_done;
+    size_t gen = 0, lo = 0, hi = 0, pending = 0;
+    unsigned char* base = nullptr;
+    bool stop = false;
+    std::atomic<size_t> next{0};
+    std::atomic<bool> bad{false};
+    auto run_round = [&](size_t l, size_t h, unsigned char* b) {
+        for (size_t i; (i = l + next.fetch_add(1)) < h;)
+            if (!fill(b + (i - l) * kStageChunk, pieces[i].src, pieces[i].n)) bad = true;
+    };
+    std::vector<std::thread> pool;
+    for (size_t k = 0; nthreads > 1 && k < nthreads; k++)
+        pool.emplace_back([&] {
+            size_t seen = 0;
+            for (;;) {
+                size_t l, h;
+                unsigned char* b;
+                {
+                    std::unique_lock<std::mutex> lk(m);
+                    cv_work.wait(lk, [&] { return stop || gen != seen; });
+                    if (stop) return;
+                    seen = gen;
+                    l = lo, h = hi, b = base;
+                }
+                run_round(l, h, b);
+                std::lock_guard<std::mutex> lk(m);
+                if (--pending == 0) cv_done.notify_one();
+            }
+        });
+    int rc = RF_OK;
+    bool used[2] = {false, false};
+    const size_t rounds = (pieces.size() + kStageSlots - 1) / kStageSlots;
+    for (size_t r = 0; r < rounds && rc == RF_OK; r++) {
+        const int half = (int)(r & 1);
+        unsigned char* b = ctx->stage + half * kStageSlots * kStageChunk;
+        // the half is free once the copies out of it two rounds ago have landed
+        if (used[half] && cudaEventSynchronize(ctx->stage_ev[half]) != cudaSuccess) {
+            rc = fail(ctx, RF_ERR_CUDA, "staged copy: %s", cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        const size_t l = r * kStageSlots, h = std::min(pieces.size(), l + kStageSlots);
+        next = 0;
+        if (pool.empty()) {
+            run_round(l, h, b);
+        } else {
+            {
+                std::lock_guard<std::mutex> lk(m);
+                lo = l, hi = h, base = b, pending = pool.size();
+                gen++;
+            }
+            cv_work.notify_all();
+            std::unique_lock<std::mutex> lk(m);
+            cv_done.wait(lk, [&] { return pending == 0; });
+        }
+        if (bad) {
+            rc = fail(ctx, RF_ERR_INVALID, "staged copy: reading the source failed");
+            break;
+        }
+        for (size_t i = l; i < h && rc == RF_OK; i++) {
+            cudaError_t e = cudaMemcpyAsync(pieces[i].dst, b + (i - l) * kStageChunk, pieces[i].n, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) rc = fail(ctx, RF_ERR_CUDA, "staged copy: %s", cudaGetErrorString(e));
+        }
+        if (cudaEventRecord(ctx->stage_ev[half], s) != cudaSuccess && rc == RF_OK)
+            rc = fail(ctx, RF_ERR_CUDA, "staged copy: event record failed");
+        used[half] = true;
+    }
+    {
+        std::lock_guard<std::mutex> lk(m);
+        stop = true;
+    }
+    cv_work.notify_all();
+    for (auto& t : pool) t.join();
+    // the ring is free for the next caller only when every copy out of it has landed
+    for (int half = 0; half < 2; half++)
+        if (used[half] && cudaEventSynchronize(ctx->stage_ev[half]) != cudaSuccess && rc == RF_OK)
+            rc = fail(ctx, RF_ERR_CUDA, "staged copy: %s", cudaGetErrorString(cudaGetLastError()));
+    return rc;
+}
+
+}  // namespace rfrt
+
+namespace {
 
 // table buffers are pool allocations ordered on the context's stream
 void free_table_mem(rf_table* t)
@@ -404,7 +527,7 @@ void free_table_mem(rf_table* t)
 namespace rfrt {
 
 int upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int64_t dim, const int32_t* sel, int32_t nsel,
-           void* stream, rf_table** out, rf_table* reuse)
+           void* stream, rf_table** out, rf_table* reuse, std::vector<HostCopy>* defer)
 {
     if (!ctx || !schema || !array || !out) return fail(ctx, RF_ERR_INVALID, "null argument");
     *out = nullptr;
@@ -465,13 +588,13 @@ int upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int6
             dc.run_ends = nullptr;
             if (want[c]) {
                 int rc;
-                if ((rc = copy_in(ctx, (void**)&dc.run_ends, &dc.re_buf, &dc.re_cap, re->buffers[1], re->length * 4, s)))
+                if ((rc = copy_in(ctx, (void**)&dc.run_ends, &dc.re_buf, &dc.re_cap, re->buffers[1], re->length * 4, s, defer)))
                     return rc;
-                if ((rc = copy_in(ctx, &dc.data, &dc.data_buf, &dc.data_cap, va->buffers[1], va->length * dc.type.size(), s)))
+                if ((rc = copy_in(ctx, &dc.data, &dc.data_buf, &dc.data_cap, va->buffers[1], va->length * dc.type.size(), s, defer)))
                     return rc;
                 if (va->n_buffers > 0 && va->buffers[0] && va->null_count != 0)
                     if ((rc = copy_in(ctx, (void**)&dc.valid, &dc.valid_buf, &dc.valid_cap, va->buffers[0],
-                                      ((va->length + 15) / 16) * 2, s)))
+                                      ((va->length + 15) / 16) * 2, s, defer)))
                         return rc;
             }
         } else {
@@ -485,11 +608,11 @@ int upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int6
             if (want[c]) {
                 int rc;
                 if (ca->n_buffers < 2) return fail(ctx, RF_ERR_INVALID, "column %lld has no value buffer", c);
-                if ((rc = copy_in(ctx, &dc.data, &dc.data_buf, &dc.data_cap, ca->buffers[1], ca->length * dc.type.size(), s)))
+                if ((rc = copy_in(ctx, &dc.data, &dc.data_buf, &dc.data_cap, ca->buffers[1], ca->length * dc.type.size(), s, defer)))
                     return rc;
                 if (ca->buffers[0] && ca->null_count != 0)
                     if ((rc = copy_in(ctx, (void**)&dc.valid, &dc.valid_buf, &dc.valid_cap, ca->buffers[0],
-                                      ((ca->length + 15) / 16) * 2, s)))
+                                      ((ca->length + 15) / 16) * 2, s, defer)))
                         return rc;
             }
         }
@@ -576,6 +699,21 @@ extern "C" int rf_table_null_count(rf_table* t, int64_t* nulls)
 {
     if (!t || !nulls) return RF_ERR_INVALID;
     *nulls = t->null_count;
+    return RF_OK;
+}
+
+extern "C" int rf_table_describe(rf_table* t, char* buf, size_t len, size_t* needed)
+{
+    if (!t) return RF_ERR_INVALID;
+    std::string text;
+    for (const DevCol& c : t->cols)
+        text += c.name + "\t" + format_of(c.type) + "\t" + (c.runend ? "runend" : "flat") + "\n";
+    if (needed) *needed = text.size() + 1;
+    if (buf && len) {
+        const size_t n = std::min(len - 1, text.size());
+        std::memcpy(buf, text.data(), n);
+        buf[n] = 0;
+    }
     return RF_OK;
 }
 

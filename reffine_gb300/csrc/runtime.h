@@ -3,6 +3,9 @@
 
 #include <cuda_runtime_api.h>
 
+#include <functional>
+#include <vector>
+
 #include "device/rf_params.h"
 #include "rf_gpu.h"
 
@@ -13,8 +16,22 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
 // fills the parameter block of a plan run; lo/hi = tiling range
 int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long long& lo, long long& hi,
                 bool may_allocate);
+// one host-to-device copy that upload() leaves to its caller (see `defer`)
+struct HostCopy {
+    void* dst;
+    const void* src;
+    size_t bytes;
+};
+// copies the columns of Arrow C data into a device table; with `defer`, the device buffers are
+// allocated but the copies are appended to *defer instead of being issued
 int upload(rf_ctx* ctx, const struct ArrowSchema* schema, const struct ArrowArray* array, int64_t dim,
-           const int32_t* sel, int32_t nsel, void* stream, rf_table** out, rf_table* reuse);
+           const int32_t* sel, int32_t nsel, void* stream, rf_table** out, rf_table* reuse,
+           std::vector<HostCopy>* defer = nullptr);
+// Issues `copies` through the context's pinned staging ring: host threads fill(dst_pinned, src,
+// bytes) chunks into one half of the ring while the other half's DMA runs.  Returns after the
+// last copy is enqueued on `s` and every staging slot it used is free again.
+int staged_h2d(rf_ctx* ctx, const std::vector<HostCopy>& copies,
+               const std::function<bool(void*, const void*, size_t)>& fill, cudaStream_t s);
 int build_index(rf_table* t, cudaStream_t s);
 void thunk_release(rf_plan* p);
 

@@ -95,18 +95,22 @@ class Engine:
         return dt
 
     def load_ipc(self, path: str, dim: int) -> "DeviceTable":
-        """Record batch 0 of an Arrow IPC file, read by the library's parser and copied straight
-        to the device (the role of load_arrow_file, src/utils/utils.cpp:11-34)."""
-        from .table import ir_type_of_c, read_ipc_c, release_c
-        s, a = read_ipc_c(path)
-        try:
-            h = ctypes.c_void_p()
-            self.check(self.lib.rf_table_upload(self.h, ctypes.byref(s), ctypes.byref(a), dim, None, ctypes.byref(h)))
-            self.sync()  # the file's memory is released next
-            names = [s.children[c].contents.name.decode() for c in range(s.n_children)]
-            return DeviceTable(self, h, ir_type_of_c(s, dim), names)
-        finally:
-            release_c(s, a)
+        """Record batch 0 of an Arrow IPC file, streamed from the file to the device by the
+        library (rf_table_load_ipc; the role of load_arrow_file, src/utils/utils.cpp:11-34)."""
+        h = ctypes.c_void_p()
+        self.check(self.lib.rf_table_load_ipc(self.h, path.encode(), dim, None, ctypes.byref(h)))
+        names, types, encs = [], [], []
+        need = ctypes.c_size_t()
+        self.check(self.lib.rf_table_describe(h, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        self.check(self.lib.rf_table_describe(h, buf, len(buf), None))
+        from .table import DTYPE_OF_FMT
+        for line in buf.value.decode().splitlines():
+            nm, fmt, enc = line.split("\t")
+            names.append(nm)
+            types.append(ir.DataType(DTYPE_OF_FMT[fmt]))
+            encs.append(ir.RUNEND if enc == "runend" else ir.FLAT)
+        return DeviceTable(self, h, ir.DataType("vector", types, dim, encs), names)
 
     def compile(self, fn: ir.Func, vectorize: bool = False) -> "Plan":
         h = ctypes.c_void_p()

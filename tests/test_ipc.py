@@ -6,8 +6,9 @@ import shutil
 import numpy as np
 import pytest
 
-from reffine_gb300 import _capi, ir
-from reffine_gb300.table import read_ipc_c, release_c, table_from_ipc, unpack_validity
+from reffine_gb300 import _capi, ir, workloads as W
+from reffine_gb300.ipc_write import write_ipc
+from reffine_gb300.table import Table, read_ipc_c, release_c, table_from_ipc, unpack_validity
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -79,3 +80,49 @@ def test_damaged_files_fail_cleanly(tmp_path):
             assert e.status in (_capi.RF_ERR_INVALID, _capi.RF_ERR_UNSUPPORTED)
     with pytest.raises(_capi.RfError, match="cannot open"):
         read_ipc_c(str(tmp_path / "missing.arrow"))
+
+
+def _types_table():
+    ref = np.load(os.path.join(GOLDEN, "ipc_types.npz"))
+    names = [n for n in ref.files if not n.startswith("valid_")]
+    return Table.from_arrays(1, {n: ref[n] for n in names}, valid={n: ref["valid_" + n] for n in names}), ref, names
+
+
+def test_writer_round_trips_through_own_reader(tmp_path):
+    # every width with nulls, and a run-end column: written by ipc_write, read by rf_ipc_read
+    t, ref, names = _types_table()
+    p = str(tmp_path / "types.arrow")
+    write_ipc(p, t)
+    back = table_from_ipc(p, 1)
+    for c, n in zip(back.columns, names):
+        m = unpack_validity(c.valid, len(c.data))
+        assert np.array_equal(m, ref["valid_" + n]) and np.array_equal(c.data[m], ref[n][m]), n
+        assert c.dtype == t.columns[names.index(n)].dtype
+    ree = W.ree_sorted(W.hashgroup_table(20_000, 700, 1.1, seed=8))
+    p = str(tmp_path / "ree.arrow")
+    write_ipc(p, ree)
+    back = table_from_ipc(p, 2)
+    assert back.columns[0].encoding == ir.RUNEND
+    assert np.array_equal(back.columns[0].run_ends, ree.columns[0].run_ends)
+    assert np.array_equal(back.columns[0].data, ree.columns[0].data)
+    assert np.array_equal(back.columns[1].data, ree.columns[1].data)
+
+
+def test_writer_output_is_valid_arrow(tmp_path):
+    pa = pytest.importorskip("pyarrow")
+    ipc = pytest.importorskip("pyarrow.ipc")
+    t, ref, names = _types_table()
+    p = str(tmp_path / "types.arrow")
+    write_ipc(p, t)
+    b = ipc.open_file(p).get_batch(0)
+    b.validate(full=True)
+    for n in names:
+        col = b.column(n)
+        m = ~col.is_null().to_numpy(zero_copy_only=False)
+        assert np.array_equal(m, ref["valid_" + n])
+        assert np.array_equal(col.to_numpy(zero_copy_only=False)[m], ref[n][m]), n
+    ree = W.ree_sorted(W.hashgroup_table(3_000, 100, 1.1, seed=9))
+    write_ipc(p, ree)
+    b = ipc.open_file(p).get_batch(0)
+    b.validate(full=True)
+    assert isinstance(b.column(0), pa.RunEndEncodedArray) and b.num_rows == 3_000
