@@ -295,7 +295,9 @@ def bench_ingest(eng, config: int, rows: int = 0, reps: int = 3):
     """Arrow IPC ingest (load_arrow_file, src/utils/utils.cpp:11-34): the config's table written
     as an IPC file (the page cache holds it after the write; disk speed is not measured), then
     host_read: rf_ipc_read, file -> host Arrow C data (what the reference's load does, CPU only);
-    load: rf_table_load_ipc, file -> HBM, streamed through the pinned staging ring;
+    load: rf_table_load_ipc, file -> HBM (on a Grace host: DMA straight out of the mapped file);
+    load_staged: the same through the pinned staging ring (the path for hosts whose GPU cannot
+    read pageable memory);
     read_then_upload: rf_ipc_read, then rf_table_upload from its pageable memory.
     The config's query runs on the loaded table and on an upload of the in-memory table: both
     results must have the same bits."""
@@ -323,6 +325,13 @@ def bench_ingest(eng, config: int, rows: int = 0, reps: int = 3):
             eng.load_ipc(path, t.dim).free()
             eng.sync()
 
+        def load_staged():
+            os.environ["RF_IPC_LOAD"] = "staged"
+            try:
+                load()
+            finally:
+                del os.environ["RF_IPC_LOAD"]
+
         def read_then_upload():
             s, a = read_ipc_c(path)
             try:
@@ -334,7 +343,8 @@ def bench_ingest(eng, config: int, rows: int = 0, reps: int = 3):
                 release_c(s, a)
 
         res = {}
-        for nm, f in (("host_read", host_read), ("load", load), ("read_then_upload", read_then_upload)):
+        for nm, f in (("host_read", host_read), ("load", load), ("load_staged", load_staged),
+                      ("read_then_upload", read_then_upload)):
             f()  # first run: allocations, staging ring, page cache settled
             ts = []
             for _ in range(reps):
@@ -481,6 +491,14 @@ def main():
         e2e = {"value": all_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": int(plan.info.output_size), "ms_per_step": e2e_s * 1e3,
                "path": "compile_op function pointer (rf_plan_thunk), pinned host tables"}
+        # the same call on the tables' own (pageable, numpy) memory, as a caller's ArrowTable2 holds it
+        q(*tables)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            q(*tables)
+        pg_s = dist.max(time.perf_counter() - t0) / args.e2e_steps
+        e2e["pageable"] = {"value": all_bytes / pg_s / 1e9, "ms_per_step": pg_s * 1e3}
         del ptables
         for b in pinned:
             b.free()

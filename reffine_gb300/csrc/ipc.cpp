@@ -16,6 +16,7 @@
 #include <unistd.h>
 
 #include <cerrno>
+#include <cstdlib>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -408,16 +409,20 @@ extern "C" int rf_ipc_read(const char* path, ArrowSchema* schema, ArrowArray* ar
     return RF_OK;
 }
 
-// The file is mapped for the parser (it touches only the footer and the message metadata) and
-// its body is streamed to the device: reader threads pread slices of the column buffers into the
-// pinned staging ring while the previous slices' DMA runs (staged_h2d).  No host copy of the
-// whole file is made.
+// The file is mapped and parsed in place (the parser touches only the footer and the message
+// metadata).  Where the GPU reads pageable memory through the host page tables (Grace hosts) the
+// mapping is populated up front and the column buffers are copied straight out of it by DMA: one
+// pass over the page cache, no host copy.  Elsewhere host threads pread slices of the column
+// buffers into the pinned staging ring while the previous slices' DMA runs (staged_h2d).
+// RF_IPC_LOAD=staged selects the second path on any host.
 extern "C" int rf_table_load_ipc(rf_ctx* ctx, const char* path, int64_t dim, void* stream, rf_table** out)
 {
     if (!ctx || !out || !path) return ctx ? rfrt::fail(ctx, RF_ERR_INVALID, "null argument") : RF_ERR_INVALID;
     *out = nullptr;
     cudaSetDevice(ctx->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    const char* mode = std::getenv("RF_IPC_LOAD");
+    const bool direct = ctx->pageable_direct && !(mode && std::strcmp(mode, "staged") == 0);
     const int fd = ::open(path, O_RDONLY | O_CLOEXEC);
     if (fd < 0) return rfrt::fail(ctx, RF_ERR_INVALID, "cannot open %s", path);
     struct stat st;
@@ -426,12 +431,12 @@ extern "C" int rf_table_load_ipc(rf_ctx* ctx, const char* path, int64_t dim, voi
         return rfrt::fail(ctx, RF_ERR_INVALID, "%s: not an Arrow IPC file (too short)", path);
     }
     const size_t size = (size_t)st.st_size;
-    void* map = ::mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
+    void* map = ::mmap(nullptr, size, PROT_READ, MAP_PRIVATE | (direct ? MAP_POPULATE : 0), fd, 0);
     if (map == MAP_FAILED) {
         ::close(fd);
         return rfrt::fail(ctx, RF_ERR_INVALID, "cannot map %s", path);
     }
-    ::posix_fadvise(fd, 0, 0, POSIX_FADV_SEQUENTIAL);
+    if (!direct) ::posix_fadvise(fd, 0, 0, POSIX_FADV_SEQUENTIAL);
     const uint8_t* base = (const uint8_t*)map;
     ArrowSchema sc;
     ArrowArray ar;
@@ -442,12 +447,19 @@ extern "C" int rf_table_load_ipc(rf_ctx* ctx, const char* path, int64_t dim, voi
         delete h;
         rc = rfrt::fail(ctx, rc, "%s", msg.c_str());
     } else {
-        std::vector<rfrt::HostCopy> copies;
-        rc = rfrt::upload(ctx, &sc, &ar, dim, nullptr, 0, s, out, nullptr, &copies);
-        if (!rc)
-            rc = rfrt::staged_h2d(ctx, copies, [&](void* dst, const void* src, size_t n) {
-                return pread_all(fd, dst, n, (size_t)((const uint8_t*)src - base));
-            }, s);
+        if (direct) {
+            rc = rfrt::upload(ctx, &sc, &ar, dim, nullptr, 0, s, out, nullptr);
+            // the mapping is unmapped next: the copies out of it must have landed
+            const cudaError_t e = cudaStreamSynchronize(s);
+            if (!rc && e != cudaSuccess) rc = rfrt::fail(ctx, RF_ERR_CUDA, "copy from %s: %s", path, cudaGetErrorString(e));
+        } else {
+            std::vector<rfrt::HostCopy> copies;
+            rc = rfrt::upload(ctx, &sc, &ar, dim, nullptr, 0, s, out, nullptr, &copies);
+            if (!rc)
+                rc = rfrt::staged_h2d(ctx, copies, [&](void* dst, const void* src, size_t n) {
+                    return pread_all(fd, dst, n, (size_t)((const uint8_t*)src - base));
+                }, s);
+        }
         if (rc && *out) {
             rf_table_free(*out);
             *out = nullptr;

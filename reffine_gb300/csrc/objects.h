@@ -89,6 +89,7 @@ struct rf_ctx {
     std::map<std::string, std::shared_ptr<JitModule>> modules;
     std::atomic<long long> launches{0};
     int sm_count = 0;
+    int pageable_direct = 0;  // cudaDevAttrPageableMemoryAccessUsesHostPageTables
     int* dev_err = nullptr;  // device error word shared by this context's launches
     // autotuner choices: tile rows per (query shape key, log2 row-count bucket)
     std::mutex tune_mu;

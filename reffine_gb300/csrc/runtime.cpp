@@ -270,6 +270,9 @@ extern "C" int rf_gpu_init(int device, rf_ctx** out)
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
     CUDA_TRY(nullptr, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
+    // Grace hosts: the GPU walks the host page tables, so copies from pageable memory run at
+    // link speed without a pinned bounce buffer
+    cudaDeviceGetAttribute(&ctx->pageable_direct, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
     CUDA_TRY(nullptr, cudaMalloc((void**)&ctx->dev_err, sizeof(int)));
     CUDA_TRY(nullptr, cudaMemset(ctx->dev_err, 0, sizeof(int)));
     *out = ctx.release();

@@ -64,3 +64,24 @@ def test_c_entry_point_and_errors(eng):
     eng.lib.rf_table_free(h)
     rc = eng.lib.rf_table_load_ipc(eng.h, os.path.join(GOLDEN, "ipc_lz4.arrow").encode(), 1, None, ctypes.byref(h))
     assert rc != 0 and b"compressed" in eng.lib.rf_last_error(eng.h)
+
+
+@pytest.mark.parametrize("path", ["default", "staged"])
+def test_large_file_loads_exactly(eng, tmp_path, monkeypatch, path):
+    # 8M rows x 36 B = 288 MB.  default: copied straight out of the populated mapping on a Grace
+    # host; staged: several rounds of the 2 x 64 MiB pinned ring, slices of every column buffer
+    # split across rounds.  Either way the loaded table gives the uploaded table's exact bits.
+    from reffine_gb300.ipc_write import write_ipc
+    if path == "staged":
+        monkeypatch.setenv("RF_IPC_LOAD", "staged")
+    t = W.filter_sum_table(8_000_003, seed=31)
+    path = str(tmp_path / "big.arrow")
+    write_ipc(path, t)
+    dt = eng.load_ipc(path, 2)
+    assert dt.nrows == len(t)
+    fn = W.filter_sum_query(t.get_data_type())
+    plan = eng.compile(fn)
+    assert plan.run(dt) == plan.run(eng.upload(t))
+    got = dt.export()
+    for c, col in enumerate(t.columns):
+        assert np.array_equal(got["cols"][c], col.data), col.name
