@@ -67,6 +67,8 @@ typedef struct RfParams {
     long long aux_n0, aux_n1;  // kernel-specific sizes
     int nunits;                // work units (virtual CTAs) of the reduction
     int flags;
+    int unit0;                 // first unit of this launch (a launch runs units unit0 .. unit0+grid-1)
+    int rsv_;
 } RfParams;
 
 #define RF_EMPTY_KEY ((long long)0x8000000000000000ULL)

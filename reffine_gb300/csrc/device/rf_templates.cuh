@@ -7,10 +7,11 @@
 //   The fragment defines: struct RfAcc (8-byte aligned fields, size a multiple of 8),
 //   rf_acc_init(P, A), rf_acc_combine(A, B) (A <- A op B), rf_acc_shfl(A, off),
 //   rf_row(P, r, A) (one row) and rf_finish(P, A, out).
-// Work is split into fixed tiles of P.tile_rows rows; unit u takes tiles u, u+nunits, ...
-// Each unit's accumulator goes to P.partials[u]; the last unit to finish folds the partials in
-// a fixed order.  So the result depends only on (rows, tile_rows, nunits, threads), not on
-// scheduling: a query gives the same bits alone or batched with others.
+// Work is split into fixed tiles of P.tile_rows rows; unit u takes the contiguous tiles
+// [u*ntiles/nunits, (u+1)*ntiles/nunits).  Each unit's accumulator goes to P.partials[u]; the
+// last unit to finish folds the partials in a fixed order.  So the result depends only on (rows,
+// tile_rows, nunits, threads), not on scheduling: a query gives the same bits alone, batched with
+// others, or launched a range of units at a time as its rows arrive (P.unit0).
 // ---------------------------------------------------------------------------------------
 #ifdef RF_SCAN_REDUCE
 template <int T>
@@ -24,7 +25,8 @@ RF_DEV void rf_scan_reduce_rows(const RfParams& P, int unit, int nunits, RfAcc& 
     }
     const long long tr = P.tile_rows;
     const long long ntiles = (P.row_hi - P.row_lo + tr - 1) / tr;
-    for (long long tile = unit; tile < ntiles; tile += nunits) {
+    const long long t_end = (long long)(unit + 1) * ntiles / nunits;
+    for (long long tile = (long long)unit * ntiles / nunits; tile < t_end; tile++) {
         long long r0 = P.row_lo + tile * tr, r1 = r0 + tr;
         if (r1 > hi) r1 = hi;
         if (r0 < lo) r0 = lo;
@@ -87,8 +89,8 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
     {                                                                                       \
         RfAcc acc;                                                                          \
         rf_acc_init(P, acc);                                                                \
-        rf_scan_reduce_rows<T>(P, blockIdx.x, gridDim.x, acc);                              \
-        rf_scan_reduce_merge<T>(P, blockIdx.x, gridDim.x, acc);                             \
+        rf_scan_reduce_rows<T>(P, P.unit0 + (int)blockIdx.x, P.nunits, acc);                \
+        rf_scan_reduce_merge<T>(P, P.unit0 + (int)blockIdx.x, P.nunits, acc);               \
     }                                                                                       \
     extern "C" __global__ void __launch_bounds__(T)                                         \
         rf_batch(const RfParams* __restrict__ params, const int2* __restrict__ work, const int* nwork) \
@@ -135,7 +137,8 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
     // per-warp queue (64 rows) behind the slots: rows passing the cheap prefix of the condition
     long long* q = (long long*)(S + (size_t)Q * T) + (size_t)warp * 64;
 #endif
-    for (long long tile = unit; tile < ntiles; tile += nunits) {
+    const long long t_end = (long long)(unit + 1) * ntiles / nunits;
+    for (long long tile = (long long)unit * ntiles / nunits; tile < t_end; tile++) {
         long long r0 = P.row_lo + tile * tr, r1 = r0 + tr;
         if (r1 > hi) r1 = hi;
         if (r0 < lo) r0 = lo;
@@ -221,7 +224,7 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
 #define RF_GROUP_REDUCE_KERNEL(NAME, T)                                                     \
     extern "C" __global__ void __launch_bounds__(T) NAME(const __grid_constant__ RfParams P) \
     {                                                                                       \
-        rf_group_reduce<T>(P, blockIdx.x, gridDim.x);                                       \
+        rf_group_reduce<T>(P, P.unit0 + (int)blockIdx.x, P.nunits);                         \
     }                                                                                       \
     extern "C" __global__ void __launch_bounds__(T)                                         \
         rf_batch(const RfParams* __restrict__ params, const int2* __restrict__ work, const int* nwork) \

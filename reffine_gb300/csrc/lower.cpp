@@ -252,6 +252,7 @@ public:
             plan_.input_types.push_back(s->type);
             plan_.cols_read.emplace_back();
             plan_.needs_index.push_back(0);
+            plan_.random_read.push_back(0);
             if (s->type.is_vector()) {
                 if (tslot >= RF_MAX_TABLES_) throw LowerError("too many table inputs");
                 if (s->type.dtypes.size() > (size_t)RF_MAX_COLS_) throw LowerError("too many columns");
@@ -503,6 +504,7 @@ private:
                     Val v = ev(r->vec);
                     if (v.k != Val::VEC) throw LowerError("readdata of a non-input vector");
                     L.note_col(v.input, r->col);
+                    L.plan_.random_read[v.input] = 1;
                     return scalar("rf_rd<" + ctype(r->type) + ">(P.t[" + std::to_string(v.slot) + "].col[" +
                                       std::to_string(r->col) + "], (long long)(" + ev(r->idx).c + "))",
                                   r->type);
@@ -517,6 +519,7 @@ private:
         std::string locate(const Val& vec, const std::string& key)
         {
             L.plan_.needs_index[vec.input] = 1;
+            L.plan_.random_read[vec.input] = 1;
             L.note_col(vec.input, 0);
             std::string call = "rf_locate(P.t[" + std::to_string(vec.slot) + "].ix, (long long)(" + key + "))";
             auto it = locate_cache.find(call);

@@ -68,6 +68,8 @@ struct Plan {
     std::vector<int> scalar_slot;       // per Func input: RfParams.s slot, or -1
     std::vector<std::vector<int>> cols_read;  // per Func input: columns the query reads
     std::vector<int> needs_index;       // per Func input: 1 if the query probes its index
+    std::vector<int> random_read;       // per Func input: 1 if rows are read at computed positions
+                                        // (ReadData, Locate), not only at the loop's own row
     std::vector<ConstSlot> consts;
     // driving loop
     HostExpr row_lo, row_hi;            // tiling range (host-known)

@@ -94,6 +94,10 @@ struct rf_ctx {
     // autotuner choices: tile rows per (query shape key, log2 row-count bucket)
     std::mutex tune_mu;
     std::map<std::string, std::map<int, long long>> tune;
+    // row-chunked runs (run_streamed): a copy stream beside `stream`, one event per chunk
+    std::mutex pipe_mu;
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> pipe_ev;
     // pinned staging ring for host copies from files and pageable memory (staged_h2d)
     std::mutex stage_mu;
     unsigned char* stage = nullptr;

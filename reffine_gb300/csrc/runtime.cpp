@@ -287,6 +287,8 @@ extern "C" int rf_gpu_shutdown(rf_ctx* ctx)
     ctx->modules.clear();
     cudaFree(ctx->dev_err);
     if (ctx->stage) cudaFreeHost(ctx->stage);
+    for (auto& e : ctx->pipe_ev) cudaEventDestroy(e);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     for (auto& e : ctx->stage_ev)
         if (e) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
@@ -374,7 +376,7 @@ namespace {
 // copies `bytes` from host `src` into the allocation (*buf, *cap), growing it if needed;
 // *active is set to the copy, or NULL when there is nothing to copy
 int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src, size_t bytes, cudaStream_t s,
-            std::vector<HostCopy>* defer)
+            std::vector<HostCopy>* defer, int width = 0)
 {
     *active = nullptr;
     if (!src || bytes == 0) return RF_OK;
@@ -388,7 +390,7 @@ int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src
         *cap = bytes;
     }
     if (defer)
-        defer->push_back({*buf, src, bytes});
+        defer->push_back({*buf, src, bytes, width});
     else
         CUDA_TRY(ctx, cudaMemcpyAsync(*buf, src, bytes, cudaMemcpyHostToDevice, s));
     *active = *buf;
@@ -611,11 +613,12 @@ int upload(rf_ctx* ctx, const ArrowSchema* schema, const ArrowArray* array, int6
             if (want[c]) {
                 int rc;
                 if (ca->n_buffers < 2) return fail(ctx, RF_ERR_INVALID, "column %lld has no value buffer", c);
-                if ((rc = copy_in(ctx, &dc.data, &dc.data_buf, &dc.data_cap, ca->buffers[1], ca->length * dc.type.size(), s, defer)))
+                if ((rc = copy_in(ctx, &dc.data, &dc.data_buf, &dc.data_cap, ca->buffers[1], ca->length * dc.type.size(), s, defer,
+                                  (int)dc.type.size())))
                     return rc;
                 if (ca->buffers[0] && ca->null_count != 0)
                     if ((rc = copy_in(ctx, (void**)&dc.valid, &dc.valid_buf, &dc.valid_cap, ca->buffers[0],
-                                      ((ca->length + 15) / 16) * 2, s, defer)))
+                                      ((ca->length + 15) / 16) * 2, s, defer, -1)))
                         return rc;
             }
         }
@@ -1244,6 +1247,115 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
     if (ixbuf) cudaFreeAsync(ixbuf, s);  // after the kernels that read it, in stream order
     if (rc) return rc;
     if (Pout) *Pout = P;
+    return RF_OK;
+}
+
+bool streamable(rf_plan* p)
+{
+    const rfg::Plan& pl = p->plan;
+    if (pl.out_is_table || pl.device_range || pl.drive_input < 0) return false;
+    if (pl.kind != rfg::PlanKind::SCAN_REDUCE && pl.kind != rfg::PlanKind::GROUP_REDUCE) return false;
+    const int d = pl.drive_input;
+    if (pl.needs_index[d] || pl.random_read[d] || pl.ixf_input == d) return false;
+    int mains = 0;
+    for (const auto& k : pl.kernels) {
+        if (index_role(k.role)) continue;
+        if (k.role != rfg::KernelSpec::MAIN) return false;
+        mains++;
+    }
+    return mains == 1;
+}
+
+int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<HostCopy>& drive, void* out)
+{
+    constexpr int kChunks = 8;
+    rf_ctx* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    if (!p->h_res && cudaHostAlloc((void**)&p->h_res, 16 + p->plan.out_size, cudaHostAllocDefault) != cudaSuccess)
+        return fail(ctx, RF_ERR_OOM, "pinned result buffer");
+    RfParams P;
+    long long lo, hi;
+    int rc = fill_params(p, args, n_args, P, lo, hi, true);
+    if (rc) return rc;
+    const rfg::Plan& pl = p->plan;
+    const long long tr = P.tile_rows;
+    const long long ntiles = (hi - lo + tr - 1) / tr;
+    const int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+    P.nunits = units;
+    size_t mi = 0;
+    while (mi < pl.kernels.size() && (index_role(pl.kernels[mi].role) || pl.kernels[mi].role != rfg::KernelSpec::MAIN)) mi++;
+    if (mi == pl.kernels.size()) return fail(ctx, RF_ERR_INVALID, "streamed run of a plan without a main kernel");
+    std::lock_guard<std::mutex> g(ctx->pipe_mu);
+    if (!ctx->copy_stream) {
+        CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        ctx->pipe_ev.assign(kChunks, nullptr);
+        for (auto& e : ctx->pipe_ev) CUDA_TRY(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    cudaStream_t cs = ctx->copy_stream;
+    void* ixbuf = nullptr;
+    if (pl.ixf_input >= 0) {
+        RfTab& tab = P.t[pl.table_slot[pl.ixf_input]];
+        rc = filtered_index(p, args[pl.ixf_input].table, P, s, &tab.ix, &ixbuf);
+    }
+    // copies start after everything enqueued on the compute stream so far (the device buffers
+    // of the driving table were allocated there)
+    if (!rc && (cudaEventRecord(ctx->pipe_ev[0], s) != cudaSuccess || cudaStreamWaitEvent(cs, ctx->pipe_ev[0], 0) != cudaSuccess))
+        rc = fail(ctx, RF_ERR_CUDA, "streamed run: ordering the copy stream");
+    const int nchunks = std::min(kChunks, units);
+    long long r0 = 0;  // rows of every driving column copied so far (the first chunk starts at row 0)
+    for (int k = 0; k < nchunks && !rc; k++) {
+        const int u0 = (int)((long long)units * k / nchunks), u1 = (int)((long long)units * (k + 1) / nchunks);
+        const bool last = k == nchunks - 1;
+        // units [u0, u1) read the rows of tiles [u0*ntiles/units, u1*ntiles/units)
+        const long long r1 = lo + (long long)u1 * ntiles / units * tr;
+        for (const HostCopy& c : drive) {
+            size_t b0, b1;
+            if (c.width == 0) {
+                if (k) continue;  // not addressable by row: whole, before the first units
+                b0 = 0, b1 = c.bytes;
+            } else if (c.width > 0) {
+                b0 = std::min(c.bytes, (size_t)r0 * (size_t)c.width);
+                b1 = last ? c.bytes : std::min(c.bytes, (size_t)r1 * (size_t)c.width);
+            } else {  // validity bitmap, read as 16-bit words: whole words, the boundary word twice
+                b0 = std::min(c.bytes, (size_t)(r0 / 16) * 2);
+                b1 = last ? c.bytes : std::min(c.bytes, (size_t)((r1 + 15) / 16) * 2);
+            }
+            if (b1 <= b0) continue;
+            const cudaError_t e = cudaMemcpyAsync((char*)c.dst + b0, (const char*)c.src + b0, b1 - b0,
+                                                  cudaMemcpyHostToDevice, cs);
+            if (e != cudaSuccess) {
+                rc = fail(ctx, RF_ERR_CUDA, "streamed run: copy: %s", cudaGetErrorString(e));
+                break;
+            }
+        }
+        if (rc) break;
+        if (cudaEventRecord(ctx->pipe_ev[k], cs) != cudaSuccess || cudaStreamWaitEvent(s, ctx->pipe_ev[k], 0) != cudaSuccess) {
+            rc = fail(ctx, RF_ERR_CUDA, "streamed run: chunk event");
+            break;
+        }
+        RfParams Q = P;
+        Q.unit0 = u0;
+        rc = launch(ctx, p->fns[mi], u1 - u0, pl.kernels[mi].threads, pl.kernels[mi].smem, s, &Q);
+        r0 = r1;
+    }
+    if (ixbuf) cudaFreeAsync(ixbuf, s);
+    if (rc) {
+        // no copy may outlive the call (the caller owns the host memory), and the units that did
+        // run left the merge ticket part-way
+        cudaStreamSynchronize(cs);
+        cudaStreamSynchronize(s);
+        cudaMemsetAsync(p->counter, 0, sizeof(unsigned int), s);
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    CUDA_TRY(ctx, cudaMemcpyAsync(p->h_res, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaMemcpyAsync(p->h_res + 16, p->dout, pl.out_size, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaStreamSynchronize(s));  // after the last chunk's event: every copy has landed too
+    int e;
+    memcpy(&e, p->h_res, sizeof(int));
+    if ((rc = device_error(ctx, e))) return rc;
+    if (out) memcpy(out, p->h_res + 16, pl.out_size);
     return RF_OK;
 }
 

@@ -21,6 +21,8 @@ struct HostCopy {
     void* dst;
     const void* src;
     size_t bytes;
+    int width;  // > 0: a flat column's values, `width` bytes per row; -1: its validity bitmap;
+                // 0: not addressable by row (run ends, run values)
 };
 // copies the columns of Arrow C data into a device table; with `defer`, the device buffers are
 // allocated but the copies are appended to *defer instead of being issued
@@ -33,6 +35,14 @@ int upload(rf_ctx* ctx, const struct ArrowSchema* schema, const struct ArrowArra
 int staged_h2d(rf_ctx* ctx, const std::vector<HostCopy>& copies,
                const std::function<bool(void*, const void*, size_t)>& fill, cudaStream_t s);
 int build_index(rf_table* t, cudaStream_t s);
+// whether a value-result plan can run while its driving table is still arriving: one main
+// kernel of a scan or grouped reduce, reading the driving table only at the loop's own rows
+bool streamable(rf_plan* p);
+// runs such a plan with the driving input's columns copied from host memory in row chunks on
+// the context's copy stream; each chunk's units launch as soon as their rows have landed.
+// `drive` = the driving input's copies as upload(..., defer) listed them.  Same units, same
+// fold order as rf_plan_run: same bits.
+int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<HostCopy>& drive, void* out);
 void thunk_release(rf_plan* p);
 
 }  // namespace rfrt

@@ -101,6 +101,10 @@ void thunk_call(int slot, void* const* a, const double* d)
     int ai = 1, di = 0;
     std::vector<rf_arg> args(pl.n_inputs);
     int rc = RF_OK;
+    // a plan that reads its driving table only row by row starts on the first rows while the
+    // rest are still being copied
+    const bool streamed = rfrt::streamable(p);
+    std::vector<rfrt::HostCopy> drive;
     for (int i = 0; i < pl.n_inputs && rc == RF_OK; i++) {
         const auto& ty = pl.input_types[i];
         rf_arg& ar = args[i];
@@ -117,7 +121,8 @@ void thunk_call(int slot, void* const* a, const double* d)
             // host-to-device copies of the referenced columns remain per call
             rf_table*& st = rfrt::staging_of(p)[i];
             rf_table* dt = nullptr;
-            rc = rfrt::upload(ctx, t->schema, t->array, t->dim, cols.data(), (int32_t)cols.size(), nullptr, &dt, st);
+            rc = rfrt::upload(ctx, t->schema, t->array, t->dim, cols.data(), (int32_t)cols.size(), nullptr, &dt, st,
+                              streamed && i == pl.drive_input ? &drive : nullptr);
             if (rc == RF_OK) st = dt;
             ar.kind = RF_ARG_TABLE;
             ar.table = dt;
@@ -171,6 +176,8 @@ void thunk_call(int slot, void* const* a, const double* d)
                     delete h;
                 }
             }
+        } else if (streamed) {
+            rc = rfrt::run_streamed(p, args.data(), (int32_t)args.size(), drive, output_addr);
         } else {
             rc = rf_plan_run(p, args.data(), (int32_t)args.size(), output_addr, nullptr);
         }
