@@ -156,7 +156,7 @@ int rf_plan_launch(rf_plan* plan, const rf_arg* args, int32_t n_args, void* dev_
 /* rf_plan_run for callers that cannot allocate device memory while running queries - a host
  * with a fixed device-memory budget decided at start-up, or a latency-critical loop where a
  * cudaMalloc/cudaFree would synchronise the device.  It allocates nothing: the plan's partial
- * results, completion counter, loop bounds and result live in one fixed array of 1 MiB that the
+ * results, completion counter, loop bounds and result live in one fixed array of 4 MiB that the
  * library holds in device memory (on every device that loads it, until the process exits);
  * runs needing more are rejected with RF_ERR_INVALID and a message saying so (the environment
  * variable RF_NOALLOC_LIMIT, in bytes, lowers that limit; it cannot raise it).  Value-output

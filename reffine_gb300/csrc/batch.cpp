@@ -168,7 +168,7 @@ extern "C" int rf_batch_add(rf_batch* b, rf_plan* plan, const rf_arg* args, int3
     int rc = fill_params(plan, args, n_args, it.P, lo, hi, true);
     if (rc) return rc;
     long long ntiles = (hi - lo + it.P.tile_rows - 1) / it.P.tile_rows;
-    it.units = (int)std::min<long long>(std::max<long long>(ntiles, 1), plan->max_units);
+    it.units = units_for(plan, ntiles);
     it.P.nunits = it.units;
     b->items.push_back(it);
     return RF_OK;

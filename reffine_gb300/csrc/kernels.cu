@@ -240,7 +240,7 @@ extern "C" int rf_k_hll(const void* keys, const unsigned short* valid, long long
 // ---------------------------------------------------------------------------------------
 #include <mutex>
 
-#define RF_NOALLOC_SCRATCH_BYTES (1u << 20)
+#define RF_NOALLOC_SCRATCH_BYTES (4u << 20)
 static __device__ __align__(256) unsigned char rf_noalloc_scratch[RF_NOALLOC_SCRATCH_BYTES];
 
 extern "C" int rf_k_noalloc_scratch(int device, void** ptr, size_t* bytes)

@@ -5,6 +5,7 @@
 #include <cuda.h>
 #include <cuda_runtime_api.h>
 
+#include <algorithm>
 #include <atomic>
 #include <map>
 #include <memory>
@@ -158,7 +159,8 @@ struct rf_plan {
     unsigned* counter = nullptr;
     long long* range = nullptr;
     unsigned char* dout = nullptr;
-    int max_units = 0;
+    int max_units = 0;                // resident blocks of the main kernel (one wave)
+    int reduce_units = 0;             // work units a reduce may be cut into (units_for)
     int thunk_slot = -1;
     long long tile_override = 0;      // set while the autotuner times a candidate
     unsigned char* h_res = nullptr;   // pinned: [error word, 16 B][value result]
@@ -190,6 +192,16 @@ struct rf_plan {
     void* seg_part = nullptr;
     size_t seg_runs_cap = 0, seg_part_cap = 0, seg_tmp_cap = 0;
 };
+
+// Work units of a value reduce over `ntiles` tiles: up to kUnitWaves waves of resident blocks.
+// Every path of a plan (alone, batched, served, row-chunked, no-alloc) takes its units from
+// here, so a query folds the same partials in the same order whichever path runs it.  Several
+// waves let a row-chunked run launch a full wave per chunk of rows.
+constexpr int kUnitWaves = 8;
+inline int units_for(const rf_plan* p, long long ntiles)
+{
+    return (int)std::min<long long>(std::max<long long>(ntiles, 1), p->reduce_units);
+}
 
 namespace {
 // Grows a device buffer to at least `bytes` (contents not kept), stream-ordered on `s`: the old

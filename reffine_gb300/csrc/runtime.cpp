@@ -925,6 +925,9 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
         }
     }
     p->max_units = ctx->sm_count * per_sm;
+    p->reduce_units = (p->plan.kind == rfg::PlanKind::SCAN_REDUCE || p->plan.kind == rfg::PlanKind::GROUP_REDUCE)
+                          ? p->max_units * kUnitWaves
+                          : p->max_units;
     if ((p->plan.kind == rfg::PlanKind::SCAN_REDUCE || p->plan.kind == rfg::PlanKind::GROUP_REDUCE) &&
         !p->plan.device_range) {
         const auto& mk = p->plan.kernels.back();
@@ -946,7 +949,7 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
     // pool (compiling many plans costs no device-wide synchronisation):
     //   [partials of the units][completion counter 64 B][loop range 64 B][value result]
     //   [table outputs: column pointer array][results 64 B]
-    p->partials_bytes = (size_t)p->max_units * (p->plan.acc_bytes ? p->plan.acc_bytes : 8);
+    p->partials_bytes = (size_t)p->reduce_units * (p->plan.acc_bytes ? p->plan.acc_bytes : 8);
     const size_t osz = p->plan.out_size ? p->plan.out_size : 8;
     auto al = [](size_t x) { return (x + 255) / 256 * 256; };
     const size_t o_counter = al(p->partials_bytes), o_range = o_counter + 256, o_out = o_range + 256;
@@ -1221,7 +1224,7 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
     if (rc) return rc;
     const rfg::Plan& pl = p->plan;
     long long ntiles = (hi - lo + P.tile_rows - 1) / P.tile_rows;
-    int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+    int units = units_for(p, ntiles);
     P.nunits = units;
     void* ixbuf = nullptr;
     if (pl.ixf_input >= 0) {
@@ -1281,7 +1284,7 @@ int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<H
     const rfg::Plan& pl = p->plan;
     const long long tr = P.tile_rows;
     const long long ntiles = (hi - lo + tr - 1) / tr;
-    const int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+    const int units = units_for(p, ntiles);
     P.nunits = units;
     size_t mi = 0;
     while (mi < pl.kernels.size() && (index_role(pl.kernels[mi].role) || pl.kernels[mi].role != rfg::KernelSpec::MAIN)) mi++;
@@ -1729,7 +1732,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         P.aux4 = p->seg_woff;
         P.aux5 = p->seg_part;
     }
-    int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+    int units = units_for(p, ntiles);
     P.nunits = units;
     for (size_t i = 0; i < pl.kernels.size(); i++) {
         const auto& k = pl.kernels[i];
@@ -1838,7 +1841,7 @@ extern "C" int rf_plan_run_noalloc(rf_plan* p, const rf_arg* args, int32_t n_arg
     int rc = fill_params(p, args, n_args, P, lo, hi, false);
     if (rc) return rc;
     long long ntiles = (hi - lo + P.tile_rows - 1) / P.tile_rows;
-    int units = (int)std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+    int units = units_for(p, ntiles);
     // layout: [counter 256][loop bounds 256][result, 256-aligned][partials: units x acc_bytes]
     size_t out_bytes = (pl.out_size + 255) / 256 * 256;
     size_t need = 512 + out_bytes + (size_t)units * pl.acc_bytes;

@@ -71,7 +71,7 @@ size_t footprint_of(rf_plan* p, long long lo, long long hi)
     long long rows = std::max<long long>(hi - lo, 0);
     if (!pl.out_is_table) {
         long long ntiles = (rows + pl.tile_rows - 1) / pl.tile_rows;
-        long long units = std::min<long long>(std::max<long long>(ntiles, 1), p->max_units);
+        long long units = units_for(p, ntiles);
         return (size_t)units * pl.acc_bytes + 2 * std::max<size_t>(pl.out_size, 16) + sizeof(RfParams);
     }
     size_t row_bytes = 8;

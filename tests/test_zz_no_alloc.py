@@ -1,6 +1,6 @@
 """rf_plan_run_noalloc: the run entry point for callers that cannot allocate device memory while
 they run queries (a fixed device-memory budget, or a loop where cudaMalloc/cudaFree would stall
-the device).  Its scratch is a fixed 1 MiB array the library holds in device memory.
+the device).  Its scratch is a fixed 4 MiB array the library holds in device memory.
 
 Checked through the C-ABI against rf_plan_run, twice in a row (the array keeps the previous
 call's contents, so the second call also shows that everything that must start from zero is
