@@ -2,6 +2,14 @@
 // query's fragment (the templates use the fragment's types and functions), once per source.
 #pragma once
 
+// independent accumulator chains of the last unit's fold over all units' partials
+#ifndef RF_FOLD
+#define RF_FOLD 16
+#endif
+#ifndef RF_FOLD_ACC
+#define RF_FOLD_ACC 4
+#endif
+
 // ---------------------------------------------------------------------------------------
 // Template 1: fused scan-filter-project-reduce.
 //   The fragment defines: struct RfAcc (8-byte aligned fields, size a multiple of 8),
@@ -60,13 +68,29 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
     if (last) {
         __threadfence();
         if (warp == 0) {
-            RfAcc tot;
-            rf_acc_init(P, tot);
-            for (int u = lane; u < nunits; u += 32) {
-                RfAcc p;
-                rf_ld_words(&p, (const RfAcc*)P.partials + u, (int)sizeof(RfAcc));
-                rf_acc_combine(tot, p);
+            // RF_FOLD_ACC independent chains per lane, combined in a fixed order (loads in flight)
+            RfAcc c[RF_FOLD_ACC];
+#pragma unroll
+            for (int k = 0; k < RF_FOLD_ACC; k++) rf_acc_init(P, c[k]);
+            int u = lane;
+            for (; u + 32 * (RF_FOLD_ACC - 1) < nunits; u += 32 * RF_FOLD_ACC) {
+#pragma unroll
+                for (int k = 0; k < RF_FOLD_ACC; k++) {
+                    RfAcc p;
+                    rf_ld_words(&p, (const RfAcc*)P.partials + u + 32 * k, (int)sizeof(RfAcc));
+                    rf_acc_combine(c[k], p);
+                }
             }
+#pragma unroll
+            for (int k = 0; k < RF_FOLD_ACC; k++)
+                if (u + 32 * k < nunits) {
+                    RfAcc p;
+                    rf_ld_words(&p, (const RfAcc*)P.partials + u + 32 * k, (int)sizeof(RfAcc));
+                    rf_acc_combine(c[k], p);
+                }
+            RfAcc tot = c[0];
+#pragma unroll
+            for (int k = 1; k < RF_FOLD_ACC; k++) rf_acc_combine(tot, c[k]);
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
                 RfAcc o = rf_acc_shfl(tot, off);
@@ -206,8 +230,23 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         __threadfence();
         for (int q = warp; q < Q; q += T / 32) {
             const int m = q % RF_M;
-            unsigned long long a = rf_slot_init(P, m);
-            for (int u = lane; u < nunits; u += 32) a = rf_slot_combine(m, a, __ldcg(part + (long long)u * Q + q));
+            // RF_FOLD independent chains per lane (chain k takes units lane + 32*(RF_FOLD*j + k)),
+            // combined in a fixed order: a lane keeps RF_FOLD loads in flight
+            unsigned long long c[RF_FOLD];
+#pragma unroll
+            for (int k = 0; k < RF_FOLD; k++) c[k] = rf_slot_init(P, m);
+            int u = lane;
+            for (; u + 32 * (RF_FOLD - 1) < nunits; u += 32 * RF_FOLD) {
+#pragma unroll
+                for (int k = 0; k < RF_FOLD; k++)
+                    c[k] = rf_slot_combine(m, c[k], __ldcg(part + (long long)(u + 32 * k) * Q + q));
+            }
+#pragma unroll
+            for (int k = 0; k < RF_FOLD; k++)
+                if (u + 32 * k < nunits) c[k] = rf_slot_combine(m, c[k], __ldcg(part + (long long)(u + 32 * k) * Q + q));
+            unsigned long long a = c[0];
+#pragma unroll
+            for (int k = 1; k < RF_FOLD; k++) a = rf_slot_combine(m, a, c[k]);
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) a = rf_slot_combine(m, a, __shfl_down_sync(0xffffffffu, a, off));
             if (lane == 0) S[q] = a;

@@ -1271,10 +1271,27 @@ bool streamable(rf_plan* p)
 
 int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<HostCopy>& drive, void* out)
 {
-    constexpr int kChunks = 8;
+    constexpr int kChunks = kUnitWaves;
     rf_ctx* ctx = p->ctx;
     cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
+    // Copies from pageable memory are not left to the copy engines alone (on this host the GPU
+    // reads pageable memory through the host page tables and competes with the chunks' kernels),
+    // so a driving table outside pinned memory is copied whole first: same units, same bits.
+    bool pinned = !drive.empty();
+    for (const HostCopy& c : drive) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, c.src) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+            cudaGetLastError();
+            pinned = false;
+            break;
+        }
+    }
+    if (!pinned) {
+        for (const HostCopy& c : drive)
+            CUDA_TRY(ctx, cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyHostToDevice, s));
+        return rf_plan_run(p, args, n_args, out, s);
+    }
     if (!p->h_res && cudaHostAlloc((void**)&p->h_res, 16 + p->plan.out_size, cudaHostAllocDefault) != cudaSuccess)
         return fail(ctx, RF_ERR_OOM, "pinned result buffer");
     RfParams P;

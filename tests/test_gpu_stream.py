@@ -9,7 +9,7 @@ from oracle import loopgen
 from parity import assert_same
 from reffine_gb300 import engine, ir, workloads as W
 from reffine_gb300.ir import _add, _f64, _func, _get, _gte, _i64, _idx, _len, _lt, _mul, _new, _red, _sel, _subvec, _sym
-from reffine_gb300.table import pack_validity
+from reffine_gb300.table import Column, Table, pack_validity
 
 pytestmark = pytest.mark.gpu
 
@@ -50,18 +50,37 @@ def case(name):
     raise KeyError(name)
 
 
+def pinned_copy(eng, t, keep):
+    """The same table with its values (and validity) in pinned host memory."""
+    cols = []
+    for c in t.columns:
+        buf = eng.host_alloc(c.data.nbytes)
+        v = buf.view(c.data.dtype, len(c.data))
+        v[:] = c.data
+        keep.append(buf)
+        cols.append(Column(c.name, c.dtype, v, c.valid, c.run_ends))
+    return Table(t.name, t.dim, cols)
+
+
 @pytest.mark.parametrize("name", ["filter_sum", "groupby", "join", "nulls", "offset"])
 def test_streamed_call_same_bits(eng, name):
     fn, tables = case(name)
+    keep = []
+    pinned = [pinned_copy(eng, t, keep) for t in tables]
     q = engine.compile_op(fn, engine=eng)
     l0 = eng.launch_count()
-    got = q(*tables)
+    got = q(*pinned)
     assert eng.launch_count() - l0 >= 2  # launched a chunk of units at a time
     plan = eng.compile(fn)
     resident = plan.run(*[eng.upload(t) for t in tables])
     assert got == resident
     assert_same(got, loopgen.Query(fn)(*tables))
-    assert q(*tables) == got  # staging buffers reused: same bits again
+    assert q(*pinned) == got  # staging buffers reused: same bits again
+    # pageable host memory takes the whole-copy path: the same bits
+    l0 = eng.launch_count()
+    assert q(*tables) == got
+    for b in keep:
+        b.free()
 
 
 def test_tiny_and_empty_tables(eng):
