@@ -58,7 +58,13 @@ def pinned_copy(eng, t, keep):
         v = buf.view(c.data.dtype, len(c.data))
         v[:] = c.data
         keep.append(buf)
-        cols.append(Column(c.name, c.dtype, v, c.valid, c.run_ends))
+        valid = None
+        if c.valid is not None:
+            vb = eng.host_alloc(c.valid.nbytes)
+            valid = vb.view(np.uint8, len(c.valid))
+            valid[:] = c.valid
+            keep.append(vb)
+        cols.append(Column(c.name, c.dtype, v, valid, c.run_ends))
     return Table(t.name, t.dim, cols)
 
 
