@@ -2,7 +2,7 @@
 // query's fragment (the templates use the fragment's types and functions), once per source.
 #pragma once
 
-// independent accumulator chains of the last unit's fold over all units' partials
+// loads a lane issues ahead of its combines in the last unit's fold over all units' partials
 #ifndef RF_FOLD
 #define RF_FOLD 16
 #endif
@@ -68,29 +68,24 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
     if (last) {
         __threadfence();
         if (warp == 0) {
-            // RF_FOLD_ACC independent chains per lane, combined in a fixed order (loads in flight)
-            RfAcc c[RF_FOLD_ACC];
-#pragma unroll
-            for (int k = 0; k < RF_FOLD_ACC; k++) rf_acc_init(P, c[k]);
+            // units lane, lane+32, ... folded in that order; their loads are issued RF_FOLD_ACC
+            // at a time ahead of the combines
+            RfAcc tot;
+            rf_acc_init(P, tot);
             int u = lane;
             for (; u + 32 * (RF_FOLD_ACC - 1) < nunits; u += 32 * RF_FOLD_ACC) {
+                RfAcc v[RF_FOLD_ACC];
 #pragma unroll
-                for (int k = 0; k < RF_FOLD_ACC; k++) {
-                    RfAcc p;
-                    rf_ld_words(&p, (const RfAcc*)P.partials + u + 32 * k, (int)sizeof(RfAcc));
-                    rf_acc_combine(c[k], p);
-                }
+                for (int k = 0; k < RF_FOLD_ACC; k++)
+                    rf_ld_words(&v[k], (const RfAcc*)P.partials + u + 32 * k, (int)sizeof(RfAcc));
+#pragma unroll
+                for (int k = 0; k < RF_FOLD_ACC; k++) rf_acc_combine(tot, v[k]);
             }
-#pragma unroll
-            for (int k = 0; k < RF_FOLD_ACC; k++)
-                if (u + 32 * k < nunits) {
-                    RfAcc p;
-                    rf_ld_words(&p, (const RfAcc*)P.partials + u + 32 * k, (int)sizeof(RfAcc));
-                    rf_acc_combine(c[k], p);
-                }
-            RfAcc tot = c[0];
-#pragma unroll
-            for (int k = 1; k < RF_FOLD_ACC; k++) rf_acc_combine(tot, c[k]);
+            for (; u < nunits; u += 32) {
+                RfAcc p;
+                rf_ld_words(&p, (const RfAcc*)P.partials + u, (int)sizeof(RfAcc));
+                rf_acc_combine(tot, p);
+            }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
                 RfAcc o = rf_acc_shfl(tot, off);
@@ -123,6 +118,10 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
         for (int w = blockIdx.x; w < n; w += gridDim.x) {                                   \
             const int2 it = work[w];                                                        \
             const RfParams& Q = params[it.x];                                               \
+            if (it.y < 0 || it.y >= Q.nunits) { /* a malformed work item: report, skip */  \
+                if (threadIdx.x == 0) atomicExch(Q.err, RF_DEVERR_RANGE);                    \
+                continue;                                                                   \
+            }                                                                               \
             RfAcc acc;                                                                      \
             rf_acc_init(Q, acc);                                                            \
             rf_scan_reduce_rows<T>(Q, it.y, Q.nunits, acc);                                 \
@@ -230,23 +229,18 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         __threadfence();
         for (int q = warp; q < Q; q += T / 32) {
             const int m = q % RF_M;
-            // RF_FOLD independent chains per lane (chain k takes units lane + 32*(RF_FOLD*j + k)),
-            // combined in a fixed order: a lane keeps RF_FOLD loads in flight
-            unsigned long long c[RF_FOLD];
-#pragma unroll
-            for (int k = 0; k < RF_FOLD; k++) c[k] = rf_slot_init(P, m);
+            // units lane, lane+32, ... folded in that order; their loads are issued RF_FOLD at a
+            // time ahead of the combines
+            unsigned long long a = rf_slot_init(P, m);
             int u = lane;
             for (; u + 32 * (RF_FOLD - 1) < nunits; u += 32 * RF_FOLD) {
+                unsigned long long v[RF_FOLD];
 #pragma unroll
-                for (int k = 0; k < RF_FOLD; k++)
-                    c[k] = rf_slot_combine(m, c[k], __ldcg(part + (long long)(u + 32 * k) * Q + q));
+                for (int k = 0; k < RF_FOLD; k++) v[k] = __ldcg(part + (long long)(u + 32 * k) * Q + q);
+#pragma unroll
+                for (int k = 0; k < RF_FOLD; k++) a = rf_slot_combine(m, a, v[k]);
             }
-#pragma unroll
-            for (int k = 0; k < RF_FOLD; k++)
-                if (u + 32 * k < nunits) c[k] = rf_slot_combine(m, c[k], __ldcg(part + (long long)(u + 32 * k) * Q + q));
-            unsigned long long a = c[0];
-#pragma unroll
-            for (int k = 1; k < RF_FOLD; k++) a = rf_slot_combine(m, a, c[k]);
+            for (; u < nunits; u += 32) a = rf_slot_combine(m, a, __ldcg(part + (long long)u * Q + q));
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) a = rf_slot_combine(m, a, __shfl_down_sync(0xffffffffu, a, off));
             if (lane == 0) S[q] = a;
@@ -271,6 +265,10 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         const int n = *nwork;                                                               \
         for (int w = blockIdx.x; w < n; w += gridDim.x) {                                   \
             const int2 it = work[w];                                                        \
+            if (it.y < 0 || it.y >= params[it.x].nunits) { /* malformed work item */       \
+                if (threadIdx.x == 0) atomicExch(params[it.x].err, RF_DEVERR_RANGE);         \
+                continue;                                                                   \
+            }                                                                               \
             rf_group_reduce<T>(params[it.x], it.y, params[it.x].nunits);                    \
         }                                                                                   \
     }
