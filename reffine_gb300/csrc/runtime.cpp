@@ -874,6 +874,18 @@ extern "C" int rf_table_export(rf_table* t, ArrowSchema* so, ArrowArray* ao)
 // ------------------------------------------------------------------------------------------
 // plans
 // ------------------------------------------------------------------------------------------
+// Waves of resident blocks a reduce's work units fill.  More units balance uneven rows (the
+// join's probe: 2.0 -> 1.6 ms at 200M rows with 8 waves) and let a row-chunked run launch a full
+// wave per chunk; but every unit folds its block's slots into a partial and the last unit folds
+// all partials, FP64 adds on GB300's narrow FP64 pipe: with 6 x 6 slots (the 60M-row group-by)
+// 8 waves cost 1.27 -> 1.47 ms.  So plans with many slots keep one wave.
+static int unit_waves(const rfg::Plan& pl)
+{
+    if (pl.kind == rfg::PlanKind::SCAN_REDUCE) return kUnitWaves;
+    if (pl.kind == rfg::PlanKind::GROUP_REDUCE) return pl.groups * pl.aggs <= 16 ? kUnitWaves : 1;
+    return 1;
+}
+
 extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_plan** out)
 {
     if (!ctx || !text || !out) return fail(ctx, RF_ERR_INVALID, "null argument");
@@ -925,9 +937,7 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
         }
     }
     p->max_units = ctx->sm_count * per_sm;
-    p->reduce_units = (p->plan.kind == rfg::PlanKind::SCAN_REDUCE || p->plan.kind == rfg::PlanKind::GROUP_REDUCE)
-                          ? p->max_units * kUnitWaves
-                          : p->max_units;
+    p->reduce_units = p->max_units * unit_waves(p->plan);
     if ((p->plan.kind == rfg::PlanKind::SCAN_REDUCE || p->plan.kind == rfg::PlanKind::GROUP_REDUCE) &&
         !p->plan.device_range) {
         const auto& mk = p->plan.kernels.back();
@@ -1279,6 +1289,18 @@ int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<H
     // reads pageable memory through the host page tables and competes with the chunks' kernels),
     // so a driving table outside pinned memory is copied whole first: same units, same bits.
     bool pinned = !drive.empty();
+    // chunks of at least one unit per SM: fewer units than that per chunk leave each chunk's
+    // kernel as long as the whole run's, and its tail is not shortened
+    int nchunks = 1;
+    {
+        RfParams P0;
+        long long lo0, hi0;
+        if (fill_params(p, args, n_args, P0, lo0, hi0, true) == RF_OK) {
+            const int u = units_for(p, (hi0 - lo0 + P0.tile_rows - 1) / P0.tile_rows);
+            nchunks = std::min(kChunks, u / std::max(1, ctx->sm_count));
+        }
+    }
+    if (nchunks < 2) pinned = false;
     for (const HostCopy& c : drive) {
         cudaPointerAttributes a;
         if (cudaPointerGetAttributes(&a, c.src) != cudaSuccess || a.type != cudaMemoryTypeHost) {
@@ -1287,7 +1309,7 @@ int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<H
             break;
         }
     }
-    if (!pinned) {
+    if (!pinned) {  // (or too few units to chunk)
         for (const HostCopy& c : drive)
             CUDA_TRY(ctx, cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyHostToDevice, s));
         return rf_plan_run(p, args, n_args, out, s);
@@ -1322,7 +1344,7 @@ int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<H
     // of the driving table were allocated there)
     if (!rc && (cudaEventRecord(ctx->pipe_ev[0], s) != cudaSuccess || cudaStreamWaitEvent(cs, ctx->pipe_ev[0], 0) != cudaSuccess))
         rc = fail(ctx, RF_ERR_CUDA, "streamed run: ordering the copy stream");
-    const int nchunks = std::min(kChunks, units);
+    nchunks = std::min(nchunks, units);
     long long r0 = 0;  // rows of every driving column copied so far (the first chunk starts at row 0)
     for (int k = 0; k < nchunks && !rc; k++) {
         const int u0 = (int)((long long)units * k / nchunks), u1 = (int)((long long)units * (k + 1) / nchunks);

@@ -32,20 +32,20 @@ def offset_sum_query(tbl_type, start):
 
 def case(name):
     if name == "filter_sum":
-        t = W.filter_sum_table(3_000_017, seed=41)
+        t = W.filter_sum_table(6_000_017, seed=41)
         return W.filter_sum_query(t.get_data_type()), [t]
     if name == "groupby":
-        t = W.groupby_table(2_500_003, seed=42)
+        t = W.groupby_table(6_000_003, seed=42)
         return W.groupby_query(t.get_data_type()), [t]
     if name == "join":
-        b, p = W.join_tables(50_000, 2_000_011, seed=43)
+        b, p = W.join_tables(50_000, 6_000_011, seed=43)
         return W.join_query(b.get_data_type(), p.get_data_type()), [b, p]
     if name == "nulls":
-        t = W.filter_sum_table(1_700_001, seed=44)
+        t = W.filter_sum_table(6_000_001, seed=44)
         t.columns[1].valid = pack_validity(np.random.default_rng(2).random(len(t)) < 0.8)
         return W.filter_sum_query(t.get_data_type()), [t]
     if name == "offset":
-        t = W.filter_sum_table(2_000_003, seed=45)
+        t = W.filter_sum_table(7_000_003, seed=45)
         return offset_sum_query(t.get_data_type(), 777_777), [t]
     raise KeyError(name)
 
