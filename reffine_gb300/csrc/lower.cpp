@@ -2111,6 +2111,13 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
     // (one 32-byte sector for up to three accumulators), so a row touches one sector.
     // Device layout: slots (unsigned long long*)P.aux4 [C + 1][RF_HG_SW] (slot C: the key
     // RF_EMPTY_KEY itself, a used flag in its key word), rows P.aux_n0, capacity C = P.aux_n1.
+    static int hg_rows_per_step()
+    {
+        const char* e = getenv("RF_HG_U");
+        const int u = e ? atoi(e) : 1;
+        return u == 1 || u == 2 || u == 4 || u == 8 ? u : 4;
+    }
+
     void lower_hash_group(const Op& op, const Drive& d, const Reduce& red)
     {
         plan_.kind = PlanKind::HASH_GROUP;
@@ -2137,7 +2144,8 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         const int SW = L + 1 <= 4 ? 4 : (L + 1 <= 8 ? 8 : 16);
         if (L + 1 > 16) throw LowerError("hash group-by with more than 15 aggregates");
         o << "#include \"rf_device.cuh\"\n\n#define RF_HG_L " << LL << "\n#define RF_HG_SW " << SW
-          << "\n#define RF_HG_T " << HT << "\n#define RF_HG_HK " << HK << "\n\n";
+          << "\n#define RF_HG_T " << HT << "\n#define RF_HG_HK " << HK << "\n#define RF_HG_U " << hg_rows_per_step()
+          << "\n#define RF_HG_SPK " << kHotSlotsPerKey << "\n\n";
         plan_.acc_bytes = (size_t)SW * 8;
         auto kind_of = [&](const Leaf& lf) -> std::string {
             bool f = lf.type.is_float() && !lf.count;
@@ -2302,13 +2310,15 @@ extern "C" __global__ void __launch_bounds__(256) rf_hg_init(const __grid_consta
 // slot's key never changes; a stale empty is corrected by the compare-and-swap).  The hot-key
 // index is a read-only table built on the host: open addressing, load <= 0.5, 32-bit
 // multiplicative hash of the folded key.
+// The hot-key table is collision-free (the host chose its hash multiplier and left out any key
+// whose slot a hotter key took), so a lookup is one probe.
 // Dynamic shared memory:
-//   hk[2HK] i64 | hid[2HK] i32 | wacc[W][HK][L] | xs[W][32][L] | seen[HK] u8
+//   hk[HKS] i64 | hid[HKS] u8 | wacc[W][HK][L] | xs[W][32][L] | seen[HK] u8,  HKS = RF_HG_SPK * HK
 // (a key is a group as soon as one valid row has it, whatever the row adds)
-RF_DEV unsigned rf_hg_h32(long long key, int bits)
+RF_DEV unsigned rf_hg_h32(long long key, unsigned mult, int bits)
 {
     const unsigned f = (unsigned)key ^ (unsigned)((unsigned long long)key >> 32);
-    return (f * 0x9E3779B1u) >> (32 - bits);
+    return (f * mult) >> (32 - bits);
 }
 
 RF_DEV long long rf_hg_slot_l1(const RfParams& P, long long key)
@@ -2333,21 +2343,22 @@ RF_DEV long long rf_hg_slot_l1(const RfParams& P, long long key)
 
 extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_constant__ RfParams P)
 {
-    constexpr int W = RF_HG_T / 32, HKS = 2 * RF_HG_HK;
+    constexpr int W = RF_HG_T / 32, HKS = RF_HG_SPK * RF_HG_HK;
     int bits = 0;
     while ((1 << bits) < HKS) bits++;
     extern __shared__ __align__(16) unsigned char smem[];
     long long* hk = (long long*)smem;
-    int* hid = (int*)(hk + HKS);
-    unsigned long long* wacc = (unsigned long long*)(smem + ((size_t)HKS * 12 + 15) / 16 * 16);
+    unsigned char* hid = (unsigned char*)(hk + HKS);
+    unsigned long long* wacc = (unsigned long long*)(smem + ((size_t)HKS * 9 + 15) / 16 * 16);
     unsigned long long* xs = wacc + (size_t)W * RF_HG_HK * RF_HG_L;
     unsigned char* seen = (unsigned char*)(xs + (size_t)W * 32 * RF_HG_L);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // the hot-key image: hk | hid (aux5; null: no hot keys)
+    // the hot-key image: multiplier | hk | hid (aux5; null: no hot keys)
     const unsigned char* img = (const unsigned char*)P.aux5;
+    const unsigned mult = img ? *(const unsigned*)img : 0x9E3779B1u;
     for (int i = tid; i < HKS; i += RF_HG_T) {
-        hk[i] = img ? ((const long long*)img)[i] : RF_EMPTY_KEY;
-        hid[i] = img ? ((const int*)(img + HKS * 8))[i] : 0;
+        hk[i] = img ? ((const long long*)(img + 8))[i] : RF_EMPTY_KEY;
+        hid[i] = img ? img[8 + (size_t)HKS * 8 + i] : 0;
     }
     for (int i = tid; i < W * RF_HG_HK * RF_HG_L; i += RF_HG_T) wacc[i] = rf_hg_identity(P, i % RF_HG_L);
     for (int i = tid; i < RF_HG_HK; i += RF_HG_T) seen[i] = 0;
@@ -2356,51 +2367,85 @@ extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_con
     unsigned long long* wa = wacc + (size_t)warp * RF_HG_HK * RF_HG_L;
     unsigned long long* x = xs + ((size_t)warp * 32 + lane) * RF_HG_L;
     const long long n = P.aux_n0;
-    // whole warps step together (the fold needs every lane); rows past the end are inactive
-    const long long wstride = (long long)gridDim.x * RF_HG_T;
-    for (long long base = ((long long)blockIdx.x * W + warp) * 32; base < n; base += wstride) {
-        const long long r = base + lane;
+    const unsigned long long C = (unsigned long long)P.aux_n1;
+    // whole warps step together (the fold needs every lane); rows past the end are inactive.  A
+    // step takes RF_HG_U rows per lane (RF_HG_U x 32 consecutive rows per warp): all their loads
+    // are issued first, then the hot-key probes, then the first global-table read of every cold
+    // row, and only then is any of it used - the latencies overlap instead of forming one chain
+    // per row
+    const long long wstride = (long long)gridDim.x * RF_HG_T * RF_HG_U;
+    for (long long base = ((long long)blockIdx.x * W + warp) * 32 * RF_HG_U; base < n; base += wstride) {
+        bool act[RF_HG_U];
+        long long key[RF_HG_U];
+        RfHgRow row[RF_HG_U];
+#pragma unroll
+        for (int j = 0; j < RF_HG_U; j++) {
+            const long long r = base + 32 * j + lane;
 )";
-        o << "        const bool act = r < n && rf_valid(" << c0 << ".valid, r);  // a null key is no group\n";
-        o << "        const long long key = act ? rf_ld<int64_t>(" << c0 << ".data, r) : RF_EMPTY_KEY;\n";
-        o << R"(        RfHgRow row;
-        if (act) rf_hg_load(P, r, row);
-        int h = -1;
-        if (act && key != RF_EMPTY_KEY) {
-            unsigned q = rf_hg_h32(key, bits);
-            for (int p = 0; p < HKS; p++) {
-                const long long cur = hk[q];
-                if (cur == key) {
-                    h = hid[q];
-                    break;
-                }
-                if (cur == RF_EMPTY_KEY) break;
-                q = (q + 1) & (HKS - 1);
+        o << "            act[j] = r < n && rf_valid(" << c0 << ".valid, r);  // a null key is no group\n";
+        o << "            key[j] = act[j] ? rf_ld<int64_t>(" << c0 << ".data, r) : RF_EMPTY_KEY;\n";
+        o << R"(            if (act[j]) rf_hg_load(P, r, row[j]);
+        }
+        int h[RF_HG_U];
+#pragma unroll
+        for (int j = 0; j < RF_HG_U; j++) {
+            const unsigned q = rf_hg_h32(key[j], mult, bits);
+            h[j] = act[j] && key[j] != RF_EMPTY_KEY && hk[q] == key[j] ? (int)hid[q] : -1;
+        }
+        // first read of each cold row's home slot, issued for all the step's rows at once
+        unsigned long long home[RF_HG_U], first[RF_HG_U];
+#pragma unroll
+        for (int j = 0; j < RF_HG_U; j++) {
+            home[j] = 0;
+            first[j] = (unsigned long long)RF_EMPTY_KEY;
+            if (act[j] && h[j] < 0 && key[j] != RF_EMPTY_KEY) {
+                home[j] = rf_home(key[j], C);
+                first[j] = __ldca(tab + home[j] * RF_HG_SW);
             }
         }
-        // fold of the hottest keys: lanes of one hot key find each other, the lowest folds
-        const unsigned peers = __match_any_sync(0xffffffffu, h >= 0 ? h : -1 - lane);
-        if (h >= 0) {
-            rf_hg_vals(P, row, x);
-            __syncwarp(peers);
-            if (lane == __ffs(peers) - 1) {
-                unsigned long long a[RF_HG_L];
 #pragma unroll
-                for (int l = 0; l < RF_HG_L; l++) a[l] = x[l];
-                for (unsigned m = peers & (peers - 1); m; m &= m - 1) {
-                    const unsigned long long* y = xs + ((size_t)warp * 32 + (__ffs(m) - 1)) * RF_HG_L;
+        for (int j = 0; j < RF_HG_U; j++) {
+            // fold of the hottest keys: lanes of one hot key find each other, the lowest folds
+            const unsigned peers = __match_any_sync(0xffffffffu, h[j] >= 0 ? h[j] : -1 - lane);
+            if (h[j] >= 0) {
+                rf_hg_vals(P, row[j], x);
+                __syncwarp(peers);
+                if (lane == __ffs(peers) - 1) {
+                    unsigned long long a[RF_HG_L];
 #pragma unroll
-                    for (int l = 0; l < RF_HG_L; l++) a[l] = rf_hg_comb(l, a[l], y[l]);
+                    for (int l = 0; l < RF_HG_L; l++) a[l] = x[l];
+                    for (unsigned m = peers & (peers - 1); m; m &= m - 1) {
+                        const unsigned long long* y = xs + ((size_t)warp * 32 + (__ffs(m) - 1)) * RF_HG_L;
+#pragma unroll
+                        for (int l = 0; l < RF_HG_L; l++) a[l] = rf_hg_comb(l, a[l], y[l]);
+                    }
+                    unsigned long long* A = wa + (size_t)h[j] * RF_HG_L;
+#pragma unroll
+                    for (int l = 0; l < RF_HG_L; l++) A[l] = rf_hg_comb(l, A[l], a[l]);
+                    seen[h[j]] = 1;
                 }
-                unsigned long long* A = wa + (size_t)h * RF_HG_L;
-#pragma unroll
-                for (int l = 0; l < RF_HG_L; l++) A[l] = rf_hg_comb(l, A[l], a[l]);
-                seen[h] = 1;
+                __syncwarp(peers);
             }
-            __syncwarp(peers);
-        } else if (act) {
-            const long long g = rf_hg_slot_l1(P, key);
-            if (g >= 0) rf_hg_apply(P, row, tab + g * RF_HG_SW + 1, 1);
+        }
+#pragma unroll
+        for (int j = 0; j < RF_HG_U; j++) {
+            if (!act[j] || h[j] >= 0) continue;
+            long long g;
+            if (key[j] == RF_EMPTY_KEY) {
+                g = rf_hg_slot_l1(P, key[j]);
+            } else if (first[j] == (unsigned long long)key[j]) {
+                g = (long long)home[j];
+            } else {
+                // the home slot is empty (claim it) or holds another key (probe on)
+                g = -1;
+                if (first[j] == (unsigned long long)RF_EMPTY_KEY) {
+                    const unsigned long long old = atomicCAS(tab + home[j] * RF_HG_SW, (unsigned long long)RF_EMPTY_KEY,
+                                                             (unsigned long long)key[j]);
+                    if (old == (unsigned long long)RF_EMPTY_KEY || old == (unsigned long long)key[j]) g = (long long)home[j];
+                }
+                if (g < 0) g = rf_hg_slot_l1(P, key[j]);
+            }
+            if (g >= 0) rf_hg_apply(P, row[j], tab + g * RF_HG_SW + 1, 1);
         }
     }
     __syncthreads();
@@ -2495,7 +2540,7 @@ extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_con
         plan_.kernels.clear();
         plan_.kernels.push_back({"rf_hg_init", 256, 0, KernelSpec::INIT});
         {
-            const size_t head = ((size_t)2 * HK * 12 + 15) / 16 * 16;
+            const size_t head = ((size_t)kHotSlotsPerKey * HK * 9 + 15) / 16 * 16;
             const size_t smem = head + ((size_t)HW * HK + (size_t)HW * 32) * LL * 8 + (size_t)(HK + 15) / 16 * 16;
             plan_.kernels.push_back({"rf_hg_agg", HT, smem, KernelSpec::MAIN});
         }

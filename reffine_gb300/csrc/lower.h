@@ -94,6 +94,9 @@ struct Plan {
 
 Plan lower(const std::shared_ptr<Func>& fn, bool vectorize);
 
+// hash group-by: slots of the shared-memory hot-key table per hot key (a power of two)
+constexpr int kHotSlotsPerKey = 16;
+
 // byte size and alignment of a value type in the C layout the reference's emitted structs use
 size_t c_size(const DataType& t);
 size_t c_align(const DataType& t);

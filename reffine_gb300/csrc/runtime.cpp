@@ -1577,12 +1577,17 @@ int hot_keys(rf_table* t, cudaStream_t s)
 // multiplicative hash of the folded key) of the HK hottest keys with ids 0..HK-1, laid out
 //   hk[2HK] i64 | hid[2HK] i32.
 // Only which rows take which path depends on it, never a result.  Null: no hot keys.
-static inline unsigned host_h32(long long key, int bits)
+static inline unsigned host_h32(long long key, unsigned mult, int bits)
 {
     const unsigned f = (unsigned)key ^ (unsigned)((unsigned long long)key >> 32);
-    return (f * 0x9E3779B1u) >> (32 - bits);
+    return (f * mult) >> (32 - bits);
 }
 
+// The hot-key image the aggregation kernel copies to shared memory:
+//   [u32 multiplier][u32 0] [i64 key of each of RF_HG_SLOTS_PER_KEY*HK slots] [u8 hot id per slot]
+// The hottest keys are placed in hotness order, each in the single slot its hash names: the kernel
+// finds a key with one probe and no loop.  Among 64 odd multipliers the one that places the most
+// keys is used; a key whose slot is taken stays cold (it takes the global table's path).
 int hot_image(rf_plan* p, rf_table* vt, cudaStream_t s, void** img)
 {
     *img = nullptr;
@@ -1602,19 +1607,34 @@ int hot_image(rf_plan* p, rf_table* vt, cudaStream_t s, void** img)
     p->hg_img_for = vt->gen;
     p->hg_img_some = !keys.empty();
     if (keys.empty()) return RF_OK;
-    const size_t HKS = 2 * (size_t)HK, bytes = HKS * 12;
+    if ((int)keys.size() > HK) keys.resize(HK);
+    const size_t HKS = (size_t)rfg::kHotSlotsPerKey * HK, bytes = 8 + HKS * 9;
     int bits = 0;
     while (((size_t)1 << bits) < HKS) bits++;
     std::vector<unsigned char> buf(bytes, 0);
-    long long* hk = (long long*)buf.data();
-    int* hid = (int*)(buf.data() + HKS * 8);
-    std::fill(hk, hk + HKS, RF_EMPTY_KEY);
-    for (size_t i = 0; i < keys.size() && (int)i < HK; i++) {
-        size_t h = host_h32(keys[i], bits);
-        while (hk[h] != RF_EMPTY_KEY) h = (h + 1) & (HKS - 1);
-        hk[h] = keys[i];
-        hid[h] = (int)i;
+    long long* hk = (long long*)(buf.data() + 8);
+    unsigned char* hid = buf.data() + 8 + HKS * 8;
+    unsigned best_mult = 0x9E3779B1u;
+    size_t best_placed = 0;
+    std::vector<char> used(HKS);
+    for (unsigned t = 0; t < 64 && best_placed < keys.size(); t++) {
+        const unsigned mult = 0x9E3779B1u + 2u * t * 0x10001u;
+        std::fill(used.begin(), used.end(), 0);
+        size_t placed = 0;
+        for (long long k : keys) {
+            const unsigned h = host_h32(k, mult, bits);
+            if (!used[h]) used[h] = 1, placed++;
+        }
+        if (placed > best_placed) best_placed = placed, best_mult = mult;
     }
+    std::fill(hk, hk + HKS, RF_EMPTY_KEY);
+    for (size_t i = 0; i < keys.size(); i++) {
+        const unsigned h = host_h32(keys[i], best_mult, bits);
+        if (hk[h] != RF_EMPTY_KEY) continue;  // taken by a hotter key: this one stays cold
+        hk[h] = keys[i];
+        hid[h] = (unsigned char)i;
+    }
+    std::memcpy(buf.data(), &best_mult, 4);
     if (!grow(&p->hg_img, &p->hg_img_cap, bytes, s)) {
         p->hg_img_for = 0;
         return fail(p->ctx, RF_ERR_OOM, "hot-key image");
