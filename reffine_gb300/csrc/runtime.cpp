@@ -1705,6 +1705,8 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         rf_table* vt = args[pl.drive_input].table;
         long long ndv = 0;
         if ((rc = ndv_estimate(vt, 0, s, &ndv))) return rc;
+        // load <= 0.45: 1.6x and 3x the distinct count measured slower (fewer slots: longer
+        // probes; more: a larger table to fill and to miss in L2)
         hg_cap = std::max<long long>(1024, (long long)(2.2 * (double)ndv));
         if (p->hg_retry_cap > hg_cap) hg_cap = p->hg_retry_cap;
         // slots of pl.acc_bytes bytes: {key, accumulators} (array of structs)
