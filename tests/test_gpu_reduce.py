@@ -129,3 +129,23 @@ def test_missing_lower_bound_reports_error(eng):
     # the context stays usable
     st = rq.students_table()
     assert eng.compile(rq.vector_op(st)).run(eng.upload(st)) == 696
+
+
+def test_groupby_fused_products_nonfinite(eng):
+    # summed values of the form x*(1-y), x*(1+y) run as one fused multiply-add; rows with an
+    # infinite or NaN factor must still give the reference's inf / NaN sums
+    t = W.groupby_table(400_003, seed=17)
+    price, disc, tax = (t.columns[i].data for i in (4, 5, 6))
+    rng = np.random.default_rng(4)
+    idx = rng.choice(len(t), 12, replace=False)
+    price[idx[0]] = np.inf
+    price[idx[1]] = -np.inf
+    price[idx[2]] = np.nan
+    disc[idx[3]] = np.inf
+    tax[idx[4]] = -np.inf
+    disc[idx[5]] = 1.0      # x*(1-y) = 0 exactly
+    price[idx[6]] = 0.0
+    disc[idx[6]] = np.inf   # 0*(1-inf): NaN
+    fn = W.groupby_query(t.get_data_type())
+    got = eng.compile(fn).run(eng.upload(t))
+    assert_same(got, loopgen.Query(fn)(t))
