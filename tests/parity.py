@@ -18,6 +18,9 @@ def assert_same(got, ref, rtol=RTOL_F64, path="out"):
         if math.isnan(ref):
             assert math.isnan(got), "%s: %r vs NaN" % (path, got)
             return
+        if math.isinf(ref):
+            assert got == ref, "%s: %r vs %r" % (path, got, ref)
+            return
         tol = rtol * max(abs(ref), 1e-300)
         assert abs(got - ref) <= tol, "%s: %r vs %r (rel %.3g)" % (path, got, ref,
                                                                    abs(got - ref) / max(abs(ref), 1e-300))
