@@ -196,20 +196,6 @@ RF_DEV void rf_set_err(const RfParams& P, int code)
 }
 
 // 8-byte words through L2 (coherent between the blocks of one grid)
-// x*(1-y) and x*(1+y) for a summed FP64 value: x - x*y and x + x*y as one fused multiply-add
-// (one rounding, one FP64 instruction instead of two; the sums are FP64 either way).  An
-// infinite or NaN x keeps the two-step form (inf - inf*y would be NaN where inf*(1-y) is not).
-RF_DEV double rf_mul_1m(double x, double y)
-{
-    if (((unsigned long long)__double_as_longlong(x) >> 52 & 0x7ffULL) == 0x7ffULL) return x * (1.0 - y);
-    return fma(-x, y, x);
-}
-RF_DEV double rf_mul_1p(double x, double y)
-{
-    if (((unsigned long long)__double_as_longlong(x) >> 52 & 0x7ffULL) == 0x7ffULL) return x * (1.0 + y);
-    return fma(x, y, x);
-}
-
 RF_DEV void rf_st_words(void* dst, const void* src, int nbytes)
 {
     unsigned long long* d = (unsigned long long*)dst;

@@ -392,21 +392,8 @@ private:
         std::map<std::string, std::string> locate_cache;
         int counter = 0;
         bool in_bounds_rows = true;
-        // x*(1-y) and x*(1+y) as one FP64 fused multiply-add (rf_mul_1m/rf_mul_1p): only in a
-        // value that is summed (ev_sum_value), never in a condition, a MIN/MAX, a projected column
-        // or a symbol's shared closure - there each row keeps the reference's two roundings
-        bool fuse = false;
 
         explicit Emitter(Lowerer& l) : L(l) {}
-
-        Val ev_sum_value(const Expr& e)
-        {
-            const bool o = fuse;
-            fuse = true;
-            Val v = ev(e);
-            fuse = o;
-            return v;
-        }
 
         std::string fresh(const std::string& b) { return b + std::to_string(counter++); }
         void bind(const Expr& s, Val v) { scopes.back().bind[s.get()] = std::move(v); }
@@ -452,10 +439,7 @@ private:
                     auto sym = std::static_pointer_cast<SymNode>(e);
                     auto it = L.fn_->tbl.find(sym);
                     if (it == L.fn_->tbl.end()) throw LowerError("unbound symbol " + sym->name, false);
-                    const bool fo = fuse;
-                    fuse = false;  // a symbol's closure is shared by every use of it
                     Val v = ev(it->second);
-                    fuse = fo;
                     if (v.k == Val::SCALAR) {
                         std::string base;
                         for (char ch : sym->name) base += isalnum((unsigned char)ch) ? ch : '_';
@@ -606,24 +590,6 @@ private:
         {
             auto a = [&](size_t i) { return ev(n.args[i]).c; };
             const std::string T = n.type.is_primitive() ? ctype(n.type) : "";
-            if (fuse && n.op == MathOp::MUL && n.type.btype == FLOAT64) {
-                // x*(1-y) -> rf_mul_1m(x, y), x*(1+y) or x*(y+1) -> rf_mul_1p(x, y), either side
-                auto is_one = [](const Expr& e) {
-                    return is_kind(e, NodeKind::CONST) && e->type.btype == FLOAT64 && as<Const>(e)->val == 1.0;
-                };
-                for (int s = 0; s < 2; s++) {
-                    const Expr& f = n.args[1 - s];
-                    if (!is_kind(f, NodeKind::NARY) || f->type.btype != FLOAT64) continue;
-                    auto fn = as<NaryExpr>(f);
-                    if (fn->args.size() != 2) continue;
-                    if (fn->op == MathOp::SUB && is_one(fn->args[0]))
-                        return scalar("rf_mul_1m(" + a(s) + ", " + ev(fn->args[1]).c + ")", n.type);
-                    if (fn->op == MathOp::ADD && is_one(fn->args[0]))
-                        return scalar("rf_mul_1p(" + a(s) + ", " + ev(fn->args[1]).c + ")", n.type);
-                    if (fn->op == MathOp::ADD && is_one(fn->args[1]))
-                        return scalar("rf_mul_1p(" + a(s) + ", " + ev(fn->args[0]).c + ")", n.type);
-                }
-            }
             switch (n.op) {
                 case MathOp::ADD: return scalar("(" + a(0) + " + " + a(1) + ")", n.type);
                 case MathOp::SUB: return scalar("(" + a(0) + " - " + a(1) + ")", n.type);
@@ -1570,7 +1536,7 @@ private:
                 std::string val;
                 if (lj.count) val = "1";
                 else if (lj.op == AggOp::OR || lj.op == AggOp::AND) val = "(long long)(" + E.ev(lj.value).c + ")";
-                else val = "(" + ctype(lj.type) + ")(" + (lj.op == AggOp::SUM ? E.ev_sum_value(lj.value) : E.ev(lj.value)).c + ")";
+                else val = "(" + ctype(lj.type) + ")(" + E.ev(lj.value).c + ")";
                 std::string e = combine_expr(lj, a, val);
                 if (lj.type.btype == FLOAT32 && lj.op == AggOp::SUM) e = "(double)((float)" + a + " + " + val + ")";
                 upd << ind << a << " = " << e << ";\n";
@@ -1928,7 +1894,7 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
             std::string val;
             if (lf.count) val = "1";
             else if (lf.op == AggOp::OR || lf.op == AggOp::AND) val = "(long long)(" + E.ev(lf.value).c + ")";
-            else val = "(" + ctype(lf.type) + ")(" + (lf.op == AggOp::SUM ? E.ev_sum_value(lf.value) : E.ev(lf.value)).c + ")";
+            else val = "(" + ctype(lf.type) + ")(" + E.ev(lf.value).c + ")";
             gb << "    V.v" << m << " = " << val << ";\n";
         }
         gb << "    return g;\n";
@@ -2233,7 +2199,7 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
             for (int k = 0; k < L; k++) {
                 auto& lf = leaves[act[k]];
                 std::string cond = lf.cond ? E.ev(order_conjuncts(lf.cond)).c : "";
-                std::string val = lf.count ? "1" : "(" + acc_ctype(lf) + ")(" + (lf.op == AggOp::SUM ? E.ev_sum_value(lf.value) : E.ev(lf.value)).c + ")";
+                std::string val = lf.count ? "1" : "(" + acc_ctype(lf) + ")(" + E.ev(lf.value).c + ")";
                 std::string call = "rf_atom_" + kind_of(lf) + "(A + " + std::to_string(k) + " * st, " + val + ")";
                 if (kind_of(lf) == "fmax" || kind_of(lf) == "fmin") call = "if (!" + call + ") rf_set_err(P, RF_DEVERR_WAIT)";
                 if (!cond.empty()) u << "    if (" << cond << ") { " << call << "; }\n";
