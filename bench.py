@@ -406,6 +406,11 @@ def main():
 
     table_out = bool(plan.info.output_is_table)
     out_rows = [0]
+    # the tiling autotuner picks the scan tile for this shape and size once, before warm-up
+    # (rf_plan_tune; every later run of the shape uses it)
+    tile_rows = None
+    if not table_out and plan.kind in (1, 2):
+        tile_rows, _ = plan.tune(*dts, reps=3)
 
     def step():
         if not table_out:
@@ -523,7 +528,8 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": name, **cfg, "bytes_per_step": nbytes, "l2": "inputs larger than L2 (no flush)"},
+                "config": {"workload": name, **cfg, "bytes_per_step": nbytes, "l2": "inputs larger than L2 (no flush)",
+                           "tile_rows": tile_rows, "tile_rows_from": "autotuner (rf_plan_tune) before warm-up"},
                 "rows_per_s": rows * world / (ms_step / 1e3),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
