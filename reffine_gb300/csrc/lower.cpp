@@ -1413,6 +1413,35 @@ private:
         return decl.str();
     }
 
+    // Loads of the driving row that a row's values read once it has passed its filter (text
+    // from position `from` on): each distinct load into one local, declared at `from`, so the
+    // compiler sees equal operands and computes a shared subexpression (price * (1 - disc) in
+    // two sums) once.  Same loads, same rounding: only repeated work goes.
+    static void hoist_value_loads(std::string& text, size_t from)
+    {
+        const std::string pat = "rf_ld<";
+        std::map<std::string, std::string> seen;
+        std::vector<std::string> order;
+        for (size_t pos = text.find(pat, from); pos != std::string::npos; pos = text.find(pat, pos + 1)) {
+            size_t e = text.find(", r)", pos);
+            if (e == std::string::npos) continue;
+            std::string call = text.substr(pos, e + 4 - pos);
+            if (call.find("P.t[") == std::string::npos || call.find('(', pat.size()) == std::string::npos) continue;
+            if (seen.count(call)) continue;
+            seen[call] = "lv" + std::to_string(order.size());
+            order.push_back(call);
+        }
+        if (order.empty()) return;
+        std::ostringstream decl;
+        for (auto& c : order) decl << "    const " << c.substr(pat.size(), c.find('>') - pat.size()) << " " << seen[c] << " = " << c << ";\n";
+        std::string tail = text.substr(from);
+        for (auto& c : order) {
+            size_t p;
+            while ((p = tail.find(c)) != std::string::npos) tail.replace(p, c.size(), seen[c]);
+        }
+        text = text.substr(0, from) + decl.str() + tail;
+    }
+
     // cost-ordered conjunction: cheap column predicates first, hash probes last
     // evaluation cost class of a condition: 1 per node, 20 per element or data read, 100 per
     // index probe (Locate)
@@ -1903,6 +1932,11 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         std::vector<std::string*> pieces{&rowcond, &gbody};
         for (auto& dd : dcls) pieces.push_back(&dd);
         std::string hoisted = hoist_row_loads(rowcond + gconds, pieces);
+        {
+            const std::string mk = "    if (g < 0) return -1;\n";
+            const size_t at = gbody.find(mk);
+            if (at != std::string::npos) hoist_value_loads(gbody, at + mk.size());
+        }
         o << "RF_DEV int rf_group(const RfParams& P, long long r, RfVals& V)\n{\n";
         o << body.str() << hoisted;
         for (auto& dcl : dcls) o << "    " << dcl << "\n";
