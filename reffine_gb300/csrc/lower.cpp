@@ -1796,20 +1796,34 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         bool ok[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) ok[j] = rf_ixf_entry(P, b + j * 256ull, k[j], r[j]);
+        // the four entries probe in rounds: each round issues their compare-and-swaps together
+        // (independent atomics in flight), then moves the ones that met a taken slot on by one
+        unsigned long long h[4];
+        bool pend[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            if (!ok[j] || !rf_ixf_keep(P, r[j])) continue;
-            unsigned long long h = rf_home(k[j], C), m = 0;
-            for (; m < C; ++m) {
-                if (atomicCAS((unsigned long long*)&t[h].x, (unsigned long long)RF_EMPTY_KEY, (unsigned long long)k[j]) ==
-                    (unsigned long long)RF_EMPTY_KEY) {
-                    t[h].y = r[j];
-                    break;
-                }
-                if (++h == C) h = 0;
-            }
-            if (m == C) rf_set_err(P, RF_DEVERR_OVERFLOW);
+            pend[j] = ok[j] && rf_ixf_keep(P, r[j]);
+            h[j] = pend[j] ? rf_home(k[j], C) : 0;
         }
+        for (unsigned long long m = 0; m < C && (pend[0] || pend[1] || pend[2] || pend[3]); ++m) {
+            unsigned long long prev[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                prev[j] = pend[j] ? atomicCAS((unsigned long long*)&t[h[j]].x, (unsigned long long)RF_EMPTY_KEY,
+                                              (unsigned long long)k[j])
+                                  : 0ULL;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (!pend[j]) continue;
+                if (prev[j] == (unsigned long long)RF_EMPTY_KEY) {
+                    t[h[j]].y = r[j];
+                    pend[j] = false;
+                } else if (++h[j] == C) {
+                    h[j] = 0;
+                }
+            }
+        }
+        if (pend[0] || pend[1] || pend[2] || pend[3]) rf_set_err(P, RF_DEVERR_OVERFLOW);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const long long r = rf_ixf_special(P);

@@ -23,6 +23,11 @@
 #include <condition_variable>
 #include <vector>
 
+#include <dlfcn.h>
+#include <execinfo.h>
+#include <signal.h>
+#include <unistd.h>
+
 #include "arrow_c.h"
 #include "device/rf_params.h"
 #include "kernels.h"
@@ -250,12 +255,93 @@ int launch(rf_ctx* ctx, CUfunction f, int grid, int block, size_t smem, cudaStre
 using namespace rfrt;
 
 // ------------------------------------------------------------------------------------------
+// crash report (opt-in diagnostics: RF_CRASH_TRACE=1 in the environment)
+// ------------------------------------------------------------------------------------------
+// On SIGSEGV / SIGBUS / SIGABRT in any thread, writes the faulting thread's native frames to
+// stderr (each with its object file and the offset inside it, for addr2line), then hands the
+// signal to the handler installed before (Python's faulthandler prints the Python frames).
+namespace {
+struct sigaction g_prev_segv, g_prev_bus, g_prev_abrt;
+
+void put_str(const char* s) { (void)!write(2, s, strlen(s)); }
+void put_hex(uintptr_t v)
+{
+    char b[19];
+    b[0] = '0';
+    b[1] = 'x';
+    for (int i = 0; i < 16; i++) b[2 + i] = "0123456789abcdef"[(v >> (60 - 4 * i)) & 15];
+    b[18] = 0;
+    put_str(b);
+}
+
+void crash_report(int sig, siginfo_t* si, void* uc)
+{
+    put_str("reffine_gb300: fatal signal ");
+    put_hex((uintptr_t)sig);
+    put_str(" at address ");
+    put_hex((uintptr_t)(si ? si->si_addr : nullptr));
+    put_str(", native frames of the faulting thread:\n");
+    void* fr[64];
+    const int n = backtrace(fr, 64);
+    for (int i = 0; i < n; i++) {
+        Dl_info di;
+        put_str("  #");
+        put_hex((uintptr_t)i);
+        put_str(" ");
+        put_hex((uintptr_t)fr[i]);
+        if (dladdr(fr[i], &di) && di.dli_fname) {
+            put_str(" ");
+            put_str(di.dli_fname);
+            put_str(" +");
+            put_hex((uintptr_t)fr[i] - (uintptr_t)di.dli_fbase);
+            if (di.dli_sname) {
+                put_str(" ");
+                put_str(di.dli_sname);
+            }
+        }
+        put_str("\n");
+    }
+    struct sigaction* prev = sig == SIGSEGV ? &g_prev_segv : sig == SIGBUS ? &g_prev_bus : &g_prev_abrt;
+    if (prev->sa_flags & SA_SIGINFO) {
+        if (prev->sa_sigaction) {
+            prev->sa_sigaction(sig, si, uc);
+            return;
+        }
+    } else if (prev->sa_handler != SIG_DFL && prev->sa_handler != SIG_IGN) {
+        prev->sa_handler(sig);
+        return;
+    }
+    signal(sig, SIG_DFL);
+    raise(sig);
+}
+
+void install_crash_report()
+{
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char* v = getenv("RF_CRASH_TRACE");
+        if (!v || !*v || *v == '0') return;
+        void* warm[2];
+        backtrace(warm, 2);  // loads the unwinder now, not inside the handler
+        struct sigaction sa {};
+        sa.sa_sigaction = crash_report;
+        sa.sa_flags = SA_SIGINFO | SA_ONSTACK;
+        sigemptyset(&sa.sa_mask);
+        sigaction(SIGSEGV, &sa, &g_prev_segv);
+        sigaction(SIGBUS, &sa, &g_prev_bus);
+        sigaction(SIGABRT, &sa, &g_prev_abrt);
+    });
+}
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
 // context
 // ------------------------------------------------------------------------------------------
 extern "C" int rf_gpu_init(int device, rf_ctx** out)
 {
     if (!out) return RF_ERR_INVALID;
     *out = nullptr;
+    install_crash_report();
     auto ctx = std::make_unique<rf_ctx>();
     ctx->device = device;
     CUDA_TRY(nullptr, cudaSetDevice(device));

@@ -132,8 +132,8 @@ def test_missing_lower_bound_reports_error(eng):
 
 
 def test_groupby_fused_products_nonfinite(eng):
-    # summed values of the form x*(1-y), x*(1+y) run as one fused multiply-add; rows with an
-    # infinite or NaN factor must still give the reference's inf / NaN sums
+    # rows with an infinite or NaN factor must give the reference's inf / NaN sums, and a
+    # product that is exactly 0 (or NaN from 0 * inf) must stay so
     t = W.groupby_table(400_003, seed=17)
     price, disc, tax = (t.columns[i].data for i in (4, 5, 6))
     rng = np.random.default_rng(4)
@@ -149,3 +149,27 @@ def test_groupby_fused_products_nonfinite(eng):
     fn = W.groupby_query(t.get_data_type())
     got = eng.compile(fn).run(eng.upload(t))
     assert_same(got, loopgen.Query(fn)(t))
+
+
+def test_groupby_mixed_signs_wide_exponents(eng):
+    # grouped FP64 sums over addends of both signs spread over ~60 binades, with tiny, huge,
+    # subnormal and signed-zero values at random rows
+    t = W.groupby_table(600_011, seed=23)
+    rng = np.random.default_rng(23)
+    qty, price = t.columns[3].data, t.columns[4].data
+    n = len(t)
+    qty[:] = rng.uniform(-1.0, 3.0, n) * 2.0 ** rng.integers(-27, 30, n)
+    price[:] = rng.uniform(-2.0, 5.0, n) * 2.0 ** rng.integers(-20, 20, n)
+    idx = rng.choice(n, 40, replace=False)
+    qty[idx[:8]] = 1e-20
+    qty[idx[8:16]] = 2.0 ** 40
+    price[idx[16:24]] = 5e-324
+    price[idx[24:32]] = -0.0
+    qty[idx[32:40]] = 0.0
+    fn = W.groupby_query(t.get_data_type())
+    plan = eng.compile(fn)
+    assert plan.kind == 2
+    dt = eng.upload(t)
+    got = plan.run(dt)
+    assert_same(got, loopgen.Query(fn)(t))
+    assert plan.run(dt) == got  # same bits on a second run
