@@ -38,6 +38,8 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# a fatal signal in the library's threads prints their native frames (reffine_gb300 crash report)
+os.environ.setdefault("RF_CRASH_TRACE", "1")
 
 METRIC = "scan GB/s vs HBM peak per query; batched p99 latency vs per-query launch"
 
@@ -291,6 +293,25 @@ def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5)
     return out
 
 
+def serving_in_child(n_queries: int, max_rows: int, device: int, timeout_s: int = 900):
+    """bench_serving in a child process on the same GPU: its server threads and CUDA graphs
+    live and end there, and this process prints its line whatever becomes of the child."""
+    env = dict(os.environ, LOCAL_RANK=str(device), RANK="0", WORLD_SIZE="1")
+    cmd = [sys.executable, os.path.abspath(__file__), "--serving-only", "--serving-queries", str(n_queries),
+           "--serving-max-rows", str(max_rows)]
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout_s, env=env, cwd=ROOT)
+    except subprocess.TimeoutExpired:
+        return {"error": "serving run exceeded %d s" % timeout_s}
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    if r.returncode == 0 and lines:
+        try:
+            return json.loads(lines[-1])
+        except ValueError:
+            pass
+    return {"error": "serving child exited with %d: %s" % (r.returncode, (r.stderr or "")[-600:])}
+
+
 def bench_ingest(eng, config: int, rows: int = 0, reps: int = 3):
     """Arrow IPC ingest (load_arrow_file, src/utils/utils.cpp:11-34): the config's table written
     as an IPC file (the page cache holds it after the write; disk speed is not measured), then
@@ -381,10 +402,19 @@ def main():
     ap.add_argument("--serving-max-rows", type=int, default=50_000_000)
     ap.add_argument("--ingest", action="store_true",
                     help="measure Arrow IPC ingest of the config's table instead (one JSON line)")
+    ap.add_argument("--serving-only", action="store_true",
+                    help="run the serving comparison alone and print its JSON object (the child process of a "
+                         "default run)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.serving_only:
+        from reffine_gb300 import engine
+        eng = engine.Engine(local)
+        print(json.dumps(bench_serving(eng, args.serving_queries, args.serving_max_rows)), flush=True)
+        eng.close()
+        return 0
     if args.ingest:
         from reffine_gb300 import engine
         eng = engine.Engine(local)
@@ -519,10 +549,7 @@ def main():
 
     serving = None
     if rank == 0 and args.serving_queries > 0 and world == 1:
-        try:
-            serving = bench_serving(eng, args.serving_queries, args.serving_max_rows)
-        except Exception as ex:  # report, do not hide
-            serving = {"error": str(ex)[:300]}
+        serving = serving_in_child(args.serving_queries, args.serving_max_rows, local)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,

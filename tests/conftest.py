@@ -5,6 +5,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
+# a fatal signal in the library's threads prints their native frames (reffine_gb300 crash report)
+os.environ.setdefault("RF_CRASH_TRACE", "1")
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 
 
