@@ -249,3 +249,19 @@ RF_DEV bool rf_atom_fmin(unsigned long long* p, double v)
 // 64-bit slot encodings
 RF_DEV unsigned long long rf_f2u(double x) { return (unsigned long long)__double_as_longlong(x); }
 RF_DEV double rf_u2f(unsigned long long x) { return __longlong_as_double((long long)x); }
+
+// ---------------------------------------------------------------------------------------
+// Bulk L2 prefetch (sm_90+): the copy engine pulls a contiguous byte range into L2; no
+// registers, no shared memory, nothing to wait for.  rf_pf prefetches the rows [r0, r1) of a
+// column of `size`-byte values, rounded inwards to whole 16-byte blocks, so it never touches
+// bytes outside the rows the caller reads.
+// ---------------------------------------------------------------------------------------
+RF_DEV void rf_pf(const void* base, long long r0, long long r1, int size)
+{
+    unsigned long long a = (unsigned long long)base + (unsigned long long)(r0 * size);
+    unsigned long long e = (unsigned long long)base + (unsigned long long)(r1 * size);
+    a = (a + 15ULL) & ~15ULL;
+    e &= ~15ULL;
+    if (r1 > r0 && e > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a)) : "memory");
+}

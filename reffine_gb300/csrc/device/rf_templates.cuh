@@ -165,6 +165,15 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         long long r0 = P.row_lo + tile * tr, r1 = r0 + tr;
         if (r1 > hi) r1 = hi;
         if (r0 < lo) r0 = lo;
+#ifdef RF_PREFETCH
+        // the next tile's rows of the row's columns into L2 while this one is read
+        if (tid == 0 && tile + 1 < t_end) {
+            const long long n0 = P.row_lo + (tile + 1) * tr;
+            long long n1 = n0 + tr;
+            if (n1 > hi) n1 = hi;
+            rf_prefetch_rows(P, n0, n1);
+        }
+#endif
 #ifdef RF_COMPACT
         // warp-uniform steps of 8 chunks of 32 rows: the cheap tests of all 8 are issued together
         constexpr int U = 8;

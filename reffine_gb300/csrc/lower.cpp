@@ -1838,6 +1838,37 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         plan_.kernels.push_back({"rf_ixf_build", 256, 0, KernelSpec::IXBUILD});
     }
 
+    // RF_PREFETCH: rf_prefetch_rows(P, r0, r1) bulk-prefetches into L2 the rows [r0, r1) of every
+    // column `row` (a row function's text) reads at the loop's own row r, i.e. every
+    // rf_ld<T>(P.t[slot].col[c].data, r).  Returns false when there is none.
+    bool emit_prefetch(std::ostringstream& src, const std::string& row, int slot)
+    {
+        static const std::map<std::string, int> sizes = {
+            {"bool", 1}, {"int8_t", 1}, {"uint8_t", 1}, {"int16_t", 2}, {"uint16_t", 2}, {"int32_t", 4},
+            {"uint32_t", 4}, {"float", 4}, {"int64_t", 8}, {"uint64_t", 8}, {"double", 8}};
+        const std::string pre = "rf_ld<", mid = "(P.t[" + std::to_string(slot) + "].col[";
+        std::vector<std::pair<std::string, int>> cols;
+        for (size_t at = row.find(pre); at != std::string::npos; at = row.find(pre, at + pre.size())) {
+            size_t te = row.find('>', at);
+            if (te == std::string::npos) break;
+            auto sz = sizes.find(row.substr(at + pre.size(), te - at - pre.size()));
+            size_t ce = row.find(", r)", te);
+            if (sz == sizes.end() || ce == std::string::npos) continue;
+            std::string arg = row.substr(te + 1, ce - te - 1);
+            if (arg.size() <= mid.size() + 5 || arg.compare(0, mid.size(), mid) != 0 ||
+                arg.compare(arg.size() - 5, 5, ".data") != 0 || arg.find_first_of(" ,()", mid.size()) != std::string::npos)
+                continue;
+            std::pair<std::string, int> c{arg.substr(1), sz->second};
+            if (std::find(cols.begin(), cols.end(), c) == cols.end()) cols.push_back(c);
+        }
+        if (cols.empty()) return false;
+        src << "#define RF_PREFETCH 1\n";
+        src << "RF_DEV void rf_prefetch_rows(const RfParams& P, long long r0, long long r1)\n{\n";
+        for (auto& c : cols) src << "    rf_pf(" << c.first << ", r0, r1, " << c.second << ");\n";
+        src << "}\n\n";
+        return true;
+    }
+
     void gen_group_reduce(std::ostringstream& src, const Reduce& red, const Drive& d, std::vector<Leaf>& leaves,
                           const std::vector<std::vector<int>>& groups, const std::vector<Expr>& key_exprs,
                           const std::vector<Expr>& filters)
@@ -1951,11 +1982,14 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
             const size_t at = gbody.find(mk);
             if (at != std::string::npos) hoist_value_loads(gbody, at + mk.size());
         }
-        o << "RF_DEV int rf_group(const RfParams& P, long long r, RfVals& V)\n{\n";
-        o << body.str() << hoisted;
-        for (auto& dcl : dcls) o << "    " << dcl << "\n";
-        o << "    if (!(" << rowcond << ")) return -1;\n";
-        o << gbody << "}\n\n";
+        std::ostringstream grp;
+        grp << "RF_DEV int rf_group(const RfParams& P, long long r, RfVals& V)\n{\n";
+        grp << body.str() << hoisted;
+        for (auto& dcl : dcls) grp << "    " << dcl << "\n";
+        grp << "    if (!(" << rowcond << ")) return -1;\n";
+        grp << gbody << "}\n\n";
+        const std::string grp_text = grp.str();
+        o << grp_text;
         // Rows reach an index probe (Locate) only through cheaper filter conjuncts: the kernel
         // then tests those first and queues the passing rows per warp, so each round of probes
         // runs on 32 rows at once rather than on the few lanes of a warp that passed
@@ -1995,6 +2029,11 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         }
 
         push_index_filter(o, red, filters);
+        // A grouped scan that reads every row's columns prefetches the next tile into L2 while it
+        // works on this one (config 1: 1.23 -> 1.15 ms; its FP64 work waited on DRAM loads).  A
+        // compacting one reads most columns only for the rows that pass its cheap test, and a
+        // one-tile filter+sum unit measured slower with its own tile prefetched (0.048 -> 0.052 ms).
+        if (!compact && d.input >= 0 && d.slot >= 0) emit_prefetch(o, grp_text, d.slot);
 
         // epilogue
         Emitter Ef(*this);
