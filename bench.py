@@ -252,7 +252,8 @@ def _cols_read_cpu(fn, input_idx):
     return sorted({int(c) for c in re.findall(r"P\.t\[%d\]\.col\[(\d+)\]" % slot, src)})
 
 
-def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5)):
+def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5), table_lanes: int = 0,
+                  table_priority: int = 0):
     """Batched serving over resident tables (config 4): the same Poisson request stream through
     the continuous-batching server and through per-query launches (one rf_plan_run per request,
     in arrival order) on the same GPU.  Rates are fractions of the per-query path's closed-loop
@@ -266,26 +267,32 @@ def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5)
     sample = set(tab[:: max(1, len(tab) // 40)])  # ~40 table results compared in full, all by row count
     alone = serve.run_alone(eng, wl.requests, sample)
     keep = ("qps", "gbps", "p50_us", "p99_us", "mean_us", "mean_batch", "failed", "mismatches", "failures")
-    slim = lambda d: {k: (round(d[k], 3) if isinstance(d[k], float) else d[k]) for k in keep}
+    r3 = lambda v: round(v, 1) if isinstance(v, float) else v
+    slim = lambda d: dict({k: (round(d[k], 3) if isinstance(d[k], float) else d[k]) for k in keep},
+                          by_shape={k: [r3(v["p50_us"]), r3(v["p99_us"])] for k, v in d["by_shape"].items()})
+    kw = {"batched": {"table_lanes": table_lanes, "table_priority": table_priority}, "per_query": {}}
     out = {"queries": len(wl.requests),
            "shapes": dict(zip(serve.SHAPES, np.bincount([r.shape for r in wl.requests], minlength=4).tolist())),
            "table_rows": "log-uniform in [1e3, %.0e], 6 tables per shape, resident" % max_rows,
            "resident_gb": round(wl.resident_bytes / 1e9, 2),
            "bytes_per_query_mb": round(sum(r.nbytes for r in wl.requests) / len(wl.requests) / 1e6, 2),
-           "server": "2 lanes x 256 queries per launch, 8 GiB scratch budget", "workload_build_s": round(t_build, 1),
+           "server": "2 lanes x 256 queries per launch, %d table lane(s) at %s stream priority, 8 GiB scratch "
+                     "budget" % (max(table_lanes, 1), "normal" if table_priority < 0 else "high"),
+           "by_shape": "[p50_us, p99_us] per query shape",
+           "workload_build_s": round(t_build, 1),
            "check": "value results bit for bit; table results by row count, %d of them key-sorted in full "
                     "(FP64 within 1e-12)" % len(sample),
            "tile_rows_tuned": wl.tuning}
     closed = {}
     for mode in ("per_query", "batched"):
-        closed[mode] = slim(serve.serve_run(eng, wl, mode, math.inf, alone, check_tables=True))
+        closed[mode] = slim(serve.serve_run(eng, wl, mode, math.inf, alone, check_tables=True, **kw[mode]))
     out["closed_loop"] = closed
     cap = closed["per_query"]["qps"]
     sweep = []
     for f in rates:
         row = {"rate_qps": round(cap * f, 1), "of_per_query_capacity": f}
         for mode in ("per_query", "batched"):
-            row[mode] = slim(serve.serve_run(eng, wl, mode, cap * f, alone, seed=40 + int(f * 10)))
+            row[mode] = slim(serve.serve_run(eng, wl, mode, cap * f, alone, seed=40 + int(f * 10), **kw[mode]))
         sweep.append(row)
     out["poisson"] = sweep
     runs = [closed[m] for m in closed] + [r[m] for r in sweep for m in ("per_query", "batched")]
@@ -293,12 +300,14 @@ def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5)
     return out
 
 
-def serving_in_child(n_queries: int, max_rows: int, device: int, timeout_s: int = 900):
+def serving_in_child(n_queries: int, max_rows: int, device: int, table_lanes: int = 0, table_priority: int = 0,
+                     timeout_s: int = 900):
     """bench_serving in a child process on the same GPU: its server threads and CUDA graphs
     live and end there, and this process prints its line whatever becomes of the child."""
     env = dict(os.environ, LOCAL_RANK=str(device), RANK="0", WORLD_SIZE="1")
     cmd = [sys.executable, os.path.abspath(__file__), "--serving-only", "--serving-queries", str(n_queries),
-           "--serving-max-rows", str(max_rows)]
+           "--serving-max-rows", str(max_rows), "--serving-table-lanes", str(table_lanes),
+           "--serving-table-priority", str(table_priority)]
     try:
         r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout_s, env=env, cwd=ROOT)
     except subprocess.TimeoutExpired:
@@ -400,6 +409,10 @@ def main():
     ap.add_argument("--serving-queries", type=int, default=10_000,
                     help="requests of the batched-serving comparison (0: skip it)")
     ap.add_argument("--serving-max-rows", type=int, default=50_000_000)
+    ap.add_argument("--serving-table-lanes", type=int, default=0,
+                    help="table-result queries the batched server runs at once (0: the server's default)")
+    ap.add_argument("--serving-table-priority", type=int, default=0,
+                    help="the batched server's table lanes: >= 0 highest stream priority (default), < 0 normal")
     ap.add_argument("--ingest", action="store_true",
                     help="measure Arrow IPC ingest of the config's table instead (one JSON line)")
     ap.add_argument("--serving-only", action="store_true",
@@ -412,7 +425,9 @@ def main():
     if args.serving_only:
         from reffine_gb300 import engine
         eng = engine.Engine(local)
-        print(json.dumps(bench_serving(eng, args.serving_queries, args.serving_max_rows)), flush=True)
+        print(json.dumps(bench_serving(eng, args.serving_queries, args.serving_max_rows,
+                                       table_lanes=args.serving_table_lanes,
+                                       table_priority=args.serving_table_priority)), flush=True)
         eng.close()
         return 0
     if args.ingest:
@@ -549,7 +564,8 @@ def main():
 
     serving = None
     if rank == 0 and args.serving_queries > 0 and world == 1:
-        serving = serving_in_child(args.serving_queries, args.serving_max_rows, local)
+        serving = serving_in_child(args.serving_queries, args.serving_max_rows, local, args.serving_table_lanes,
+                                   args.serving_table_priority)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,

@@ -216,6 +216,10 @@ typedef struct rf_server_config {
     int32_t queue_capacity;   /* pending requests; 0: 65536 */
     int64_t hbm_budget_bytes; /* device scratch in flight; 0: 8 GiB */
     int32_t lane_share_pct;   /* a lane's launch fills at most this % of the block slots; 0: 75 */
+    int32_t table_lanes;      /* batched mode: table-result queries running at once; 0: 1 */
+    int32_t table_priority;   /* table-result lanes' streams: >= 0 the device's highest priority
+                                 (default: their long single queries are not held behind batch
+                                 blocks), < 0 normal priority */
     int32_t reserved_;
 } rf_server_config;
 typedef struct rf_completion {

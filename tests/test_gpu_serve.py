@@ -52,6 +52,15 @@ def test_mixed_results_equal_alone(eng, wl, alone, mode, rate):
         assert summ["mean_batch"] > 1.5  # queries were actually packed together
 
 
+def test_table_lanes_results_equal_alone(eng, wl, alone):
+    # three table-result lanes (high stream priority, the default): hash group-bys run beside each other
+    # (never two runs of one plan at once) and beside the batches; results unchanged
+    summ = serve.serve_run(eng, wl, "batched", math.inf, alone, check_tables=True, lanes=2, max_batch=64,
+                           table_lanes=3)
+    assert summ["failed"] == 0
+    assert summ["mismatches"] == 0
+
+
 def test_small_budget_and_one_lane(eng, wl, alone):
     # a budget below most requests' scratch: they run one at a time, results unchanged
     summ = serve.serve_run(eng, wl, "batched", math.inf, alone, check_tables=True, lanes=1, max_batch=8,
