@@ -220,7 +220,8 @@ typedef struct rf_server_config {
     int32_t table_priority;   /* table-result lanes' streams: >= 0 the device's highest priority
                                  (default: their long single queries are not held behind batch
                                  blocks), < 0 normal priority */
-    int32_t reserved_;
+    int32_t table_share_pct;  /* a table lane's hash aggregation fills at most this % of the block
+                                 slots, leaving room for the batch lanes; 0: 100 */
 } rf_server_config;
 typedef struct rf_completion {
     uint64_t tag;             /* the submitter's tag */

@@ -35,7 +35,7 @@ class RfServerConfig(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("max_batch", ctypes.c_int32), ("lanes", ctypes.c_int32),
                 ("queue_capacity", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
                 ("lane_share_pct", ctypes.c_int32), ("table_lanes", ctypes.c_int32),
-                ("table_priority", ctypes.c_int32), ("reserved_", ctypes.c_int32)]
+                ("table_priority", ctypes.c_int32), ("table_share_pct", ctypes.c_int32)]
 
 
 class RfCompletion(ctypes.Structure):

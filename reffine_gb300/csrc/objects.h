@@ -228,6 +228,9 @@ int check_device_error(rf_ctx* ctx);
 int device_error(rf_ctx* ctx, int e);  // RF_OK for 0, else clears the context's error word and fails
 long long tile_rows_for(rf_plan* p, long long rows);  // the tiling a run of `rows` rows uses
 void batch_set_share(rf_batch* b, int pct);
+// runs from this thread size a hash aggregation's grid at pct % of its resident blocks (a serving
+// table lane leaves room for the batch lanes; grid-stride kernel, results do not depend on it)
+void set_thread_grid_share(int pct);
 int cu_fail(rf_ctx* ctx, CUresult r, const char* what);
 }  // namespace rfrt
 

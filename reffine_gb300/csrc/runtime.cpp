@@ -254,6 +254,11 @@ int launch(rf_ctx* ctx, CUfunction f, int grid, int block, size_t smem, cudaStre
 
 using namespace rfrt;
 
+namespace {
+thread_local int t_grid_share = 100;  // set_thread_grid_share
+}
+void rfrt::set_thread_grid_share(int pct) { t_grid_share = std::min(100, std::max(1, pct)); }
+
 // ------------------------------------------------------------------------------------------
 // crash report (opt-in diagnostics: RF_CRASH_TRACE=1 in the environment)
 // ------------------------------------------------------------------------------------------
@@ -1919,7 +1924,8 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         if (k.role == rfg::KernelSpec::SEGCOUNT || k.role == rfg::KernelSpec::SEGREDUCE ||
             k.role == rfg::KernelSpec::INIT)
             grid = ctx->sm_count * 8;
-        if (pl.kind == rfg::PlanKind::HASH_GROUP && k.role == rfg::KernelSpec::MAIN) grid = p->max_units;
+        if (pl.kind == rfg::PlanKind::HASH_GROUP && k.role == rfg::KernelSpec::MAIN)
+            grid = std::max(1, p->max_units * t_grid_share / 100);
         if (k.role == rfg::KernelSpec::RANGE || k.role == rfg::KernelSpec::SCAN) grid = 1;
         if (k.role == rfg::KernelSpec::STOP)
             grid = (int)std::min<long long>(std::max<long long>((hi - lo + 255) / 256, 1), ctx->sm_count * 8);

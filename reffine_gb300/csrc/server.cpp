@@ -250,6 +250,7 @@ void sched_loop(rf_server* S)
 void solo_loop(rf_server* S, std::deque<Req>* q, cudaStream_t stream)
 {
     cudaSetDevice(S->ctx->device);
+    if (S->cfg.mode == RF_SERVE_BATCHED) set_thread_grid_share(S->cfg.table_share_pct);
     auto busy = [&](rf_plan* p) {
         return std::find(S->solo_busy.begin(), S->solo_busy.end(), p) != S->solo_busy.end();
     };
@@ -314,6 +315,7 @@ extern "C" int rf_server_create(rf_ctx* ctx, const rf_server_config* cfg, rf_ser
     if (c.hbm_budget_bytes <= 0) c.hbm_budget_bytes = (int64_t)8 << 30;
     if (c.lane_share_pct <= 0 || c.lane_share_pct > 100) c.lane_share_pct = 75;
     if (c.table_lanes <= 0) c.table_lanes = 1;
+    if (c.table_share_pct <= 0 || c.table_share_pct > 100) c.table_share_pct = 100;
     if (c.table_lanes > 16) c.table_lanes = 16;
     if (c.mode == RF_SERVE_PER_QUERY) c.table_lanes = 1;  // the baseline: one call at a time
     if (c.mode != RF_SERVE_BATCHED && c.mode != RF_SERVE_PER_QUERY)

@@ -32,14 +32,14 @@ class Server:
 
     def __init__(self, eng: Engine, mode: str = "batched", max_batch: int = 256, lanes: int = 2,
                  queue_capacity: int = 1 << 16, hbm_budget_bytes: int = 8 << 30, lane_share_pct: int = 75,
-                 table_lanes: int = 0, table_priority: int = 0):
+                 table_lanes: int = 0, table_priority: int = 0, table_share_pct: int = 0):
         self.eng = eng
         cfg = _capi.RfServerConfig()
         cfg.mode = {"batched": _capi.RF_SERVE_BATCHED, "per_query": _capi.RF_SERVE_PER_QUERY}[mode]
         cfg.max_batch, cfg.lanes, cfg.queue_capacity, cfg.hbm_budget_bytes = max_batch, lanes, queue_capacity, \
             hbm_budget_bytes
         cfg.lane_share_pct = lane_share_pct
-        cfg.table_lanes, cfg.table_priority = table_lanes, table_priority
+        cfg.table_lanes, cfg.table_priority, cfg.table_share_pct = table_lanes, table_priority, table_share_pct
         h = ctypes.c_void_p()
         eng.check(eng.lib.rf_server_create(eng.h, ctypes.byref(cfg), ctypes.byref(h)))
         self.h = h
