@@ -453,9 +453,11 @@ def main():
     out_rows = [0]
     # the tiling autotuner picks the scan tile for this shape and size once, before warm-up
     # (rf_plan_tune; every later run of the shape uses it)
-    tile_rows = None
+    tile_rows = hash_slots = None
     if not table_out and plan.kind in (1, 2):
         tile_rows, _ = plan.tune(*dts, reps=3)
+    elif plan.kind == 5:  # hash group-by: the table's slots per 100 distinct keys
+        hash_slots, _ = plan.tune(*dts, reps=2)
 
     def step():
         if not table_out:
@@ -572,7 +574,8 @@ def main():
                 "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": name, **cfg, "bytes_per_step": nbytes, "l2": "inputs larger than L2 (no flush)",
-                           "tile_rows": tile_rows, "tile_rows_from": "autotuner (rf_plan_tune) before warm-up"},
+                           "tile_rows": tile_rows, "hash_slots_per_100_keys": hash_slots,
+                           "tuning_from": "autotuner (rf_plan_tune) before warm-up"},
                 "rows_per_s": rows * world / (ms_step / 1e3),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,

@@ -22,7 +22,7 @@
  *                                   a host function pointer with the generated function's signature
  *   rf_batch_*                      no counterpart: batching of many queries into one persistent launch
  *   rf_server_*                     no counterpart: continuous-batching request loop
- *   rf_plan_tune, rf_tune_*         no counterpart: tiling autotuner
+ *   rf_plan_tune, rf_tune_*         no counterpart: autotuner (scan tiling, hash-table sizing)
  *   rf_ipc_read, rf_table_load_ipc  load_arrow_file (src/utils/utils.cpp:11-34), without Arrow C++
  *   rf_last_error                   no counterpart: the reference exits or aborts on errors
  *                                   (src/engine/cuda_engine.cpp:10-23)
@@ -191,10 +191,13 @@ int rf_batch_poll(rf_batch* b, int32_t* done);
 int rf_batch_reset(rf_batch* b);
 
 /* ---- autotuner (no reference counterpart) --------------------------------------------------
- * Times the tiling of a Reduce scan (rows per unit of work, 1K..32K) on the given inputs and
- * records the fastest for the plan's query shape and the input's log2 row-count bucket; every
- * later run of that shape and bucket in this context (alone, batched, served) uses it.  The
- * table of choices is exported and imported as text lines "shape-key bucket tile-rows". */
+ * Times, on the given inputs, the tiling of a Reduce scan (rows per unit of work, 1K..32K), or
+ * the table sizing of a hash group-by (160, 220 or 300 slots per 100 estimated distinct keys),
+ * and records the fastest for the plan's query shape and the input's log2 row-count bucket;
+ * every later run of that shape and bucket in this context (alone, batched, served) uses it.
+ * *tile_rows receives the choice (tile rows, or slots per 100 keys).  Other table-output plans
+ * are refused (RF_ERR_UNSUPPORTED).  The table of choices is exported and imported as text lines
+ * "shape-key bucket choice". */
 int rf_plan_tune(rf_plan* plan, const rf_arg* args, int32_t n_args, int32_t reps, int64_t* tile_rows, double* ms);
 int rf_tune_export(rf_ctx* ctx, char* buf, size_t len, size_t* needed);
 int rf_tune_import(rf_ctx* ctx, const char* text);

@@ -179,6 +179,7 @@ struct rf_plan {
     void* hg_acc = nullptr;
     size_t hg_keys_cap = 0, hg_acc_cap = 0;
     long long hg_retry_cap = 0;
+    int hg_factor_override = 0;       // set while the autotuner times a hash-table sizing
     void* hg_img = nullptr;           // hot-key image of the last input table (device)
     size_t hg_img_cap = 0;
     unsigned long long hg_img_for = 0;  // generation of the table the image was built for
@@ -227,6 +228,7 @@ int fail(rf_ctx* ctx, int code, const char* fmt, ...);
 int check_device_error(rf_ctx* ctx);
 int device_error(rf_ctx* ctx, int e);  // RF_OK for 0, else clears the context's error word and fails
 long long tile_rows_for(rf_plan* p, long long rows);  // the tiling a run of `rows` rows uses
+int hg_factor_for(rf_plan* p, long long rows);        // hash group-by slots per 100 distinct keys
 void batch_set_share(rf_batch* b, int pct);
 // runs from this thread size a hash aggregation's grid at pct % of its resident blocks (a serving
 // table lane leaves room for the batch lanes; grid-stride kernel, results do not depend on it)

@@ -8,6 +8,7 @@
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -1154,6 +1155,21 @@ namespace rfrt {
 // autotuner's choice for their shape and size bucket when there is one (rf_plan_tune); every
 // path of a query (alone, batched, without allocation) asks here, so all use the same tiling and
 // give the same result bits.
+// A hash group-by's table: slots per 100 estimated distinct keys, the autotuner's choice for the
+// plan's query shape and row-count bucket (the same tuning table as the scans' tiling), else 220
+// (load 0.45, the best of 160 / 220 / 300 / 400 measured on 100M Zipf(1.1) rows).
+int hg_factor_for(rf_plan* p, long long rows)
+{
+    if (p->hg_factor_override > 0) return p->hg_factor_override;
+    int bucket = 0;
+    while (bucket < 62 && (1LL << (bucket + 1)) <= rows) bucket++;
+    std::lock_guard<std::mutex> g(p->ctx->tune_mu);
+    auto it = p->ctx->tune.find(p->plan.key);
+    if (it == p->ctx->tune.end()) return 220;
+    auto jt = it->second.find(bucket);
+    return jt == it->second.end() ? 220 : (int)jt->second;
+}
+
 long long tile_rows_for(rf_plan* p, long long rows)
 {
     const rfg::Plan& pl = p->plan;
@@ -1507,6 +1523,58 @@ std::vector<rf_table*>& staging_of(rf_plan* p)
 // ------------------------------------------------------------------------------------------
 // autotuner
 // ------------------------------------------------------------------------------------------
+// Hash group-by: times whole runs (each one's output freed) with the table at 160, 220 and 300
+// slots per 100 estimated distinct keys and records the fastest, as slots per 100 keys, for the
+// plan's query shape and the input's row-count bucket.  Its output's rows and their per-key
+// counts do not depend on the sizing; a key's FP64 sum depends on the order its rows meet its
+// slot in any case (atomics), and stays within the oracle's tolerance.
+namespace {
+int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaStream_t s);
+}
+
+static int tune_hash_table(rf_plan* p, const rf_arg* args, int n_args, int reps, int64_t* choice, double* ms)
+{
+    rf_ctx* ctx = p->ctx;
+    const rfg::Plan& pl = p->plan;
+    if (pl.drive_input < 0 || pl.drive_input >= n_args || !args || args[pl.drive_input].kind != RF_ARG_TABLE ||
+        !args[pl.drive_input].table)
+        return fail(ctx, RF_ERR_INVALID, "hash group-by tuning needs its input table");
+    const long long rows = args[pl.drive_input].table->cols.empty() ? 0 : args[pl.drive_input].table->cols[0].logical;
+    cudaStream_t s = ctx->stream;
+    int best = 0, rc = RF_OK;
+    double best_ms = 0;
+    for (int f : {160, 220, 300}) {
+        p->hg_factor_override = f;
+        std::vector<double> v;
+        for (int r = 0; r <= reps && !rc; r++) {
+            rf_table* out = nullptr;
+            const auto t0 = std::chrono::steady_clock::now();
+            rc = run_table(p, args, n_args, &out, s);
+            if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = fail(ctx, RF_ERR_CUDA, "autotuner timing");
+            const double x = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            if (out) rf_table_free(out);
+            if (r) v.push_back(x);  // the first run is a warm-up
+        }
+        if (rc) break;
+        std::sort(v.begin(), v.end());
+        if (!best || v[v.size() / 2] < best_ms) {
+            best = f;
+            best_ms = v[v.size() / 2];
+        }
+    }
+    p->hg_factor_override = 0;
+    if (rc) return rc;
+    int bucket = 0;
+    while (bucket < 62 && (1LL << (bucket + 1)) <= rows) bucket++;
+    {
+        std::lock_guard<std::mutex> g(ctx->tune_mu);
+        ctx->tune[pl.key][bucket] = best;
+    }
+    if (choice) *choice = best;
+    if (ms) *ms = best_ms;
+    return RF_OK;
+}
+
 extern "C" int rf_plan_tune(rf_plan* p, const rf_arg* args, int32_t n_args, int32_t reps, int64_t* tile_rows,
                             double* ms)
 {
@@ -1514,9 +1582,11 @@ extern "C" int rf_plan_tune(rf_plan* p, const rf_arg* args, int32_t n_args, int3
     rf_ctx* ctx = p->ctx;
     cudaSetDevice(ctx->device);
     const rfg::Plan& pl = p->plan;
-    if (pl.out_is_table || (pl.kind != rfg::PlanKind::SCAN_REDUCE && pl.kind != rfg::PlanKind::GROUP_REDUCE))
-        return fail(ctx, RF_ERR_UNSUPPORTED, "the autotuner tunes the tiling of Reduce scans");
     if (reps < 1) reps = 3;
+    if (pl.kind == rfg::PlanKind::HASH_GROUP) return tune_hash_table(p, args, n_args, reps, tile_rows, ms);
+    if (pl.out_is_table || (pl.kind != rfg::PlanKind::SCAN_REDUCE && pl.kind != rfg::PlanKind::GROUP_REDUCE))
+        return fail(ctx, RF_ERR_UNSUPPORTED,
+                    "the autotuner tunes the tiling of Reduce scans and the table sizing of hash group-bys");
     RfParams P;
     long long lo, hi;
     int rc = fill_params(p, args, n_args, P, lo, hi, true);
@@ -1791,14 +1861,14 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     if (rc) return rc;
     long long hg_cap = 0;
     if (pl.kind == rfg::PlanKind::HASH_GROUP) {
-        // hash table at load factor 0.5 of the estimated distinct keys (10% margin);
-        // a probe overflow reruns with twice the capacity
+        // hash table of hg_factor_for() slots per 100 estimated distinct keys (default 220: load
+        // 0.45, i.e. 0.5 with a 10% margin on the estimate); a probe overflow reruns with twice
+        // the capacity
         rf_table* vt = args[pl.drive_input].table;
         long long ndv = 0;
         if ((rc = ndv_estimate(vt, 0, s, &ndv))) return rc;
-        // load <= 0.45: 1.6x and 3x the distinct count measured slower (fewer slots: longer
-        // probes; more: a larger table to fill and to miss in L2)
-        hg_cap = std::max<long long>(1024, (long long)(2.2 * (double)ndv));
+        const int factor = hg_factor_for(p, vt->cols[0].logical);
+        hg_cap = std::max<long long>(1024, (long long)((double)factor / 100.0 * (double)ndv));
         if (p->hg_retry_cap > hg_cap) hg_cap = p->hg_retry_cap;
         // slots of pl.acc_bytes bytes: {key, accumulators} (array of structs)
         if (!grow(&p->hg_keys, &p->hg_keys_cap, (size_t)(hg_cap + 1) * pl.acc_bytes, s))

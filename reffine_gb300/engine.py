@@ -118,7 +118,8 @@ class Engine:
         return Plan(self, h, fn, vectorize)
 
     def tune_export(self) -> str:
-        """The autotuner's choices as text lines "shape-key bucket tile-rows"."""
+        """The autotuner's choices as text lines "shape-key bucket choice" (tile rows for a Reduce
+        scan, hash-table slots per 100 distinct keys for a hash group-by)."""
         need = ctypes.c_size_t()
         self.check(self.lib.rf_tune_export(self.h, None, 0, ctypes.byref(need)))
         buf = ctypes.create_string_buffer(need.value)
@@ -131,16 +132,18 @@ class Engine:
     def tune_save(self, path: str):
         """Persists the autotuner's choices as JSON (entries keyed by query shape and size bucket)."""
         import json
-        entries = [{"shape": k, "bucket": int(b), "tile_rows": int(t)}
+        entries = [{"shape": k, "bucket": int(b), "choice": int(t)}
                    for k, b, t in (l.split() for l in self.tune_export().splitlines() if l.strip())]
         with open(path, "w") as f:
-            json.dump({"version": 1, "entries": entries}, f, indent=1)
+            json.dump({"version": 2, "entries": entries}, f, indent=1)
 
     def tune_load(self, path: str):
         import json
         with open(path) as f:
             d = json.load(f)
-        self.tune_import("".join("%s %d %d\n" % (e["shape"], e["bucket"], e["tile_rows"]) for e in d["entries"]))
+        # version 1 files name the choice "tile_rows" (they held scan tilings only)
+        self.tune_import("".join("%s %d %d\n" % (e["shape"], e["bucket"], e.get("choice", e.get("tile_rows")))
+                                 for e in d["entries"]))
 
     def host_alloc(self, nbytes: int) -> "PinnedBuffer":
         return PinnedBuffer(self, nbytes)
@@ -300,8 +303,9 @@ class Plan:
         return self._out_ct()
 
     def tune(self, *inputs, reps: int = 3):
-        """Autotunes the scan tiling for these inputs' size bucket (rf_plan_tune); returns
-        (tile_rows, ms of the fastest)."""
+        """Autotunes this query shape for these inputs' size bucket (rf_plan_tune): the tiling of
+        a Reduce scan, the table sizing of a hash group-by; returns (choice, ms of the fastest) -
+        tile rows, or hash-table slots per 100 distinct keys."""
         args = self.args(*inputs)
         t, ms = ctypes.c_int64(), ctypes.c_double()
         self.eng.check(self.eng.lib.rf_plan_tune(self.h, args, len(inputs), reps, ctypes.byref(t), ctypes.byref(ms)))

@@ -1,11 +1,14 @@
 """The tiling autotuner: its choice is used by every later run of the query shape and size
 bucket (alone and batched alike, so the results keep the same bits), results stay within the
 oracle's tolerance, and the choices survive export/import and the JSON file."""
+import numpy as np
 import pytest
 
+import refqueries as rq
 from oracle import loopgen
 from parity import assert_same
 from reffine_gb300 import engine, workloads as W
+from test_gpu_materialize import plan_run_table
 
 pytestmark = pytest.mark.gpu
 
@@ -43,8 +46,30 @@ def test_tune_filter_sum_and_groupby(eng, tmp_path):
     eng2.close()
 
 
-def test_tune_rejects_table_outputs(eng):
-    t = W.hashgroup_table(10_000, 100, seed=43)
+def test_tune_hash_group_by_table_sizing(eng):
+    # a hash group-by tunes its table's slots per 100 distinct keys; the output keeps its rows
+    # and counts, FP64 sums within the oracle's tolerance, and the choice is exported
+    t = W.hashgroup_table(400_003, 20_000, seed=43)
     plan = eng.compile(W.hashgroup_query(t.get_data_type()))
+    assert plan.kind == 5
+    before = plan_run_table(eng, plan, t)
+    choice, ms = plan.tune(eng.upload(t), reps=2)
+    assert choice in (160, 220, 300) and ms > 0
+    after = plan_run_table(eng, plan, t)
+    assert before["len"] == after["len"]
+    order_b = np.argsort(before["cols"][0])
+    order_a = np.argsort(after["cols"][0])
+    np.testing.assert_array_equal(before["cols"][0][order_b], after["cols"][0][order_a])
+    for c in range(1, len(after["cols"])):
+        if np.issubdtype(after["cols"][c].dtype, np.floating):
+            np.testing.assert_allclose(after["cols"][c][order_a], before["cols"][c][order_b], rtol=1e-12, atol=0)
+        else:
+            np.testing.assert_array_equal(after["cols"][c][order_a], before["cols"][c][order_b])
+    assert any(l.split()[-1] == str(choice) for l in eng.tune_export().splitlines())
+
+
+def test_tune_rejects_other_table_outputs(eng):
+    st = rq.students_table()
+    plan = eng.compile(rq.transform_op(st, 5, 10))
     with pytest.raises(RuntimeError, match="UNSUPPORTED"):
-        plan.tune(eng.upload(t))
+        plan.tune(eng.upload(st))
