@@ -89,7 +89,7 @@ int grow_dev(rf_ctx* ctx, void** p, size_t* cap, size_t bytes, cudaStream_t last
     *p = nullptr;
     *cap = 0;
     bytes += bytes / 2;  // room to grow
-    if (cudaMallocAsync(p, bytes, s) != cudaSuccess)
+    if (pool_alloc(p, bytes, s) != cudaSuccess)
         return fail(ctx, RF_ERR_OOM, "batch device buffer (%zu bytes)", bytes);
     *cap = bytes;
     return RF_OK;

@@ -204,6 +204,28 @@ inline int units_for(const rf_plan* p, long long ntiles)
     return (int)std::min<long long>(std::max<long long>(ntiles, 1), p->reduce_units);
 }
 
+// cudaMallocAsync from the device's stream-ordered pool.  The pool keeps freed blocks (its release
+// threshold is unlimited, so per-run buffers are reused without going back to the driver); when it
+// cannot grow any more, its unused memory is handed back to the device and the allocation is tried
+// again - first once `s`'s work is done, then once the whole device's is.
+inline cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s)
+{
+    cudaError_t e = cudaMallocAsync(p, bytes, s);
+    if (e != cudaErrorMemoryAllocation) return e;
+    cudaGetLastError();
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) return e;
+    cudaStreamSynchronize(s);
+    cudaMemPoolTrimTo(pool, 0);
+    e = cudaMallocAsync(p, bytes, s);
+    if (e != cudaErrorMemoryAllocation) return e;
+    cudaGetLastError();
+    cudaDeviceSynchronize();
+    cudaMemPoolTrimTo(pool, 0);
+    return cudaMallocAsync(p, bytes, s);
+}
+
 namespace {
 // Grows a device buffer to at least `bytes` (contents not kept), stream-ordered on `s`: the old
 // buffer is released after the work already queued on `s`, and nothing synchronises the device
@@ -215,7 +237,7 @@ bool grow(void** buf, size_t* cap, size_t bytes, cudaStream_t s)
     if (*buf) cudaFreeAsync(*buf, s);
     *buf = nullptr;
     *cap = 0;
-    if (cudaMallocAsync(buf, bytes, s) != cudaSuccess) return false;
+    if (pool_alloc(buf, bytes, s) != cudaSuccess) return false;
     *cap = bytes;
     return true;
 }

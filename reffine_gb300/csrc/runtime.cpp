@@ -477,8 +477,8 @@ int copy_in(rf_ctx* ctx, void** active, void** buf, size_t* cap, const void* src
         *buf = nullptr;
         *cap = 0;
         // 16 bytes of slack: vector loads may touch the tail of the last element's 16-byte line
-        if (cudaMallocAsync(buf, bytes + 16, s) != cudaSuccess)
-            return fail(ctx, RF_ERR_OOM, "cudaMallocAsync(%zu) failed", bytes);
+        if (pool_alloc(buf, bytes + 16, s) != cudaSuccess)
+            return fail(ctx, RF_ERR_OOM, "device allocation of %zu bytes failed", bytes);
         *cap = bytes;
     }
     if (defer)
@@ -736,9 +736,9 @@ int build_index(rf_table* t, cudaStream_t s)
     if (t->ix_special) cudaFreeAsync(t->ix_special, s);
     t->ix_slots = nullptr;
     t->ix_special = nullptr;
-    if (cudaMallocAsync((void**)&t->ix_slots, cap * 16, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
+    if (pool_alloc((void**)&t->ix_slots, cap * 16, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
     // [empty-key row, 8 B][repeated-key flag, 4 B]
-    if (cudaMallocAsync((void**)&t->ix_special, 16, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
+    if (pool_alloc((void**)&t->ix_special, 16, s) != cudaSuccess) return fail(ctx, RF_ERR_OOM, "index allocation failed");
     t->ix_cap = cap;
     t->ix_unique = -1;
     int e = rf_k_index_build(c0.data, c0.valid, c0.nvals, t->ix_slots, cap, t->ix_special, ctx->dev_err,
@@ -1058,7 +1058,7 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
     const size_t o_ptrs = o_out + al(osz), o_res = o_ptrs + al(sizeof(void*) * 2 * RF_MAX_COLS);
     const size_t total = p->plan.out_is_table ? o_res + 256 : o_ptrs;
     unsigned char* base = nullptr;
-    CUDA_TRY(ctx, cudaMallocAsync((void**)&base, total, ctx->stream));
+    CUDA_TRY(ctx, pool_alloc((void**)&base, total, ctx->stream));
     p->buf = base;
     p->partials = base;
     p->counter = (unsigned*)(base + o_counter);
@@ -1297,7 +1297,7 @@ int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, R
     int rc;
     if (p->ixf_for != T->gen) {
         unsigned long long* cnt = nullptr;
-        CUDA_TRY(ctx, cudaMallocAsync((void**)&cnt, 8, s));
+        CUDA_TRY(ctx, pool_alloc((void**)&cnt, 8, s));
         CUDA_TRY(ctx, cudaMemsetAsync(cnt, 0, 8, s));
         RfParams Q = P;
         Q.aux2 = cnt;
@@ -1314,7 +1314,7 @@ int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, R
     }
     unsigned long long cap = 64;
     while (cap < 2 * (unsigned long long)p->ixf_count) cap *= 2;
-    if (cudaMallocAsync(buf, cap * 16 + 256, s) != cudaSuccess) {
+    if (pool_alloc(buf, cap * 16 + 256, s) != cudaSuccess) {
         *buf = nullptr;
         return fail(ctx, RF_ERR_OOM, "filtered index (%llu slots)", cap);
     }
@@ -1705,7 +1705,7 @@ int hot_keys(rf_table* t, cudaStream_t s)
     std::vector<long long> h((size_t)std::max<long long>(m, 0));
     if (m > 0) {
         long long* d = nullptr;
-        CUDA_TRY(ctx, cudaMallocAsync((void**)&d, (size_t)m * 8, s));
+        CUDA_TRY(ctx, pool_alloc((void**)&d, (size_t)m * 8, s));
         int e = rf_k_sample_keys(dc.data, dc.valid, n, m, d, s);
         cudaError_t ce = (cudaError_t)e;
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(h.data(), d, (size_t)m * 8, cudaMemcpyDeviceToHost, s);
@@ -1817,7 +1817,7 @@ int ndv_estimate(rf_table* t, int col, cudaStream_t s, long long* out)
     }
     DevCol& dc = t->cols[col];
     unsigned* regs = nullptr;
-    CUDA_TRY(ctx, cudaMallocAsync((void**)&regs, RF_HLL_M * sizeof(unsigned), s));
+    CUDA_TRY(ctx, pool_alloc((void**)&regs, RF_HLL_M * sizeof(unsigned), s));
     int e = rf_k_hll(dc.data, dc.valid, dc.nvals, regs, s);
     if (e) {
         cudaFreeAsync(regs, s);
@@ -1855,6 +1855,20 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
 {
     rf_ctx* ctx = p->ctx;
     const rfg::Plan& pl = p->plan;
+    // a hash group-by's table lives for the run only (see below); an overflow's rerun grows it
+    // first, and whichever table is current when the outermost run returns goes back to the pool
+    struct ReleaseHashTable {
+        rf_plan* p;
+        cudaStream_t s;
+        ~ReleaseHashTable()
+        {
+            if (p->hg_keys) cudaFreeAsync(p->hg_keys, s);
+            p->hg_keys = nullptr;
+            p->hg_keys_cap = 0;
+        }
+    };
+    std::unique_ptr<ReleaseHashTable> release_hash;
+    if (pl.kind == rfg::PlanKind::HASH_GROUP) release_hash.reset(new ReleaseHashTable{p, s});
     RfParams P;
     long long lo, hi;
     int rc = fill_params(p, args, n_args, P, lo, hi, true);
@@ -1870,7 +1884,10 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         const int factor = hg_factor_for(p, vt->cols[0].logical);
         hg_cap = std::max<long long>(1024, (long long)((double)factor / 100.0 * (double)ndv));
         if (p->hg_retry_cap > hg_cap) hg_cap = p->hg_retry_cap;
-        // slots of pl.acc_bytes bytes: {key, accumulators} (array of structs)
+        // slots of pl.acc_bytes bytes: {key, accumulators} (array of structs).  The table is
+        // taken from the pool for this run and handed back when the run ends (stream-ordered):
+        // a serving mix holds thousands of hash group-by plans (one per query's constants), and
+        // each keeping its table measured 52 GB for 722 plans.
         if (!grow(&p->hg_keys, &p->hg_keys_cap, (size_t)(hg_cap + 1) * pl.acc_bytes, s))
             return fail(ctx, RF_ERR_OOM, "hash table allocation (%lld slots)", hg_cap);
         P.aux4 = p->hg_keys;
@@ -1899,14 +1916,14 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
             dc.name = (c < (size_t)pl.out_dim ? "it" : "out") +
                       std::to_string(c < (size_t)pl.out_dim ? c : c - pl.out_dim);
             size_t bytes = (size_t)std::max<long long>(rows, 1) * dc.type.size();
-            if (cudaMallocAsync(&dc.data_buf, bytes + 16, s) != cudaSuccess)
+            if (pool_alloc(&dc.data_buf, bytes + 16, s) != cudaSuccess)
                 return fail(ctx, RF_ERR_OOM, "output column allocation (%zu bytes) failed", bytes);
             dc.data_cap = bytes;
             dc.data = dc.data_buf;
             hptrs[c] = dc.data_buf;
             if (pl.vectorize) {
                 size_t vb = (size_t)((std::max<long long>(rows, 1) + 31) / 32) * 4;
-                if (cudaMallocAsync(&dc.valid_buf, vb + 16, s) != cudaSuccess)
+                if (pool_alloc(&dc.valid_buf, vb + 16, s) != cudaSuccess)
                     return fail(ctx, RF_ERR_OOM, "output bitmap allocation failed");
                 dc.valid_cap = vb;
                 CUDA_TRY(ctx, cudaMemsetAsync(dc.valid_buf, 0, vb + 16, s));

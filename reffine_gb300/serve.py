@@ -212,9 +212,7 @@ def build_workload(eng: Engine, n_queries: int = 10_000, tables_per_shape: int =
     if tune:
         # the autotuner's tiling for each Reduce shape and table size (one representative query
         # each; the choice applies to every query of the shape and size bucket).  The hash
-        # group-bys keep the default table sizing here: tuned to 300 slots per 100 keys their
-        # tables are larger, and a 10k-request sweep then ran out of device memory (see the
-        # serving notes on memory held across runs)
+        # group-bys keep the default table sizing here
         for r in wl.requests:
             if r.plan.info.output_is_table:
                 continue
