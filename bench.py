@@ -4,7 +4,7 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1] [--impl ours|reference]
 
 A step is one run of the query over its whole synthetic table.  Default workload: the
-low-cardinality group-by (60M rows, 6 groups; config 1 of the benchmark set).  Metric: scan
+low-cardinality group-by (60M rows, 6 groups; --config 1).  Metric: scan
 GB/s = algorithmic bytes (each referenced column read once) / time.
 
   value      kernel throughput with the table resident in HBM (CUDA events on the launch stream)
@@ -254,7 +254,7 @@ def _cols_read_cpu(fn, input_idx):
 
 def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5), table_lanes: int = 0,
                   table_priority: int = 0):
-    """Batched serving over resident tables (config 4): the same Poisson request stream through
+    """Batched serving over resident tables (10k mixed requests): the same Poisson request stream through
     the continuous-batching server and through per-query launches (one rf_plan_run per request,
     in arrival order) on the same GPU.  Rates are fractions of the per-query path's closed-loop
     capacity.  Every result is compared with the query run alone."""

@@ -2030,9 +2030,11 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
 
         push_index_filter(o, red, filters);
         // A grouped scan that reads every row's columns prefetches the next tile into L2 while it
-        // works on this one (config 1: 1.23 -> 1.15 ms; its FP64 work waited on DRAM loads).  A
-        // compacting one reads most columns only for the rows that pass its cheap test, and a
-        // one-tile filter+sum unit measured slower with its own tile prefetched (0.048 -> 0.052 ms).
+        // works on this one (the 60M-row, 6-group group-by: 1.23 -> 1.15 ms; its FP64 work waited
+        // on DRAM loads).  A compacting one reads most columns only for the rows that pass its
+        // cheap test (the 200M-row join's probe scan measured 1.45 -> 1.70 ms with a prefetch: it
+        // needs L2 for its filtered index), and a one-tile filter+sum unit measured slower with its
+        // own tile prefetched (0.048 -> 0.052 ms).
         if (!compact && d.input >= 0 && d.slot >= 0) emit_prefetch(o, grp_text, d.slot);
 
         // epilogue
