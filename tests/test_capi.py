@@ -69,6 +69,23 @@ def test_join_lowers_to_grouped_template_with_probe():
     assert "#define RF_G 5" in src
 
 
+def test_only_full_row_grouped_scans_prefetch_the_next_tile():
+    # the grouped scan that reads every row's columns asks for the next tile in L2 (every column it
+    # reads at the loop's row, whole 16-byte blocks); the join's compacting scan and the one-tile
+    # filter+sum scan measured slower with a prefetch and have none
+    g = W.groupby_table(64)
+    src = engine.check(W.groupby_query(g.get_data_type()))
+    assert "#define RF_PREFETCH 1" in src
+    body = src[src.index("rf_prefetch_rows"):]
+    body = body[:body.index("}")]
+    cols = {int(c) for c in re.findall(r"rf_pf\(P\.t\[0\]\.col\[(\d+)\]\.data", body)}
+    assert cols == {1, 2, 3, 4, 5, 6, 7}
+    b, p = W.join_tables(64, 256)
+    assert "RF_PREFETCH" not in engine.check(W.join_query(b.get_data_type(), p.get_data_type()))
+    t = W.filter_sum_table(64)
+    assert "RF_PREFETCH" not in engine.check(W.filter_sum_query(t.get_data_type()))
+
+
 @pytest.mark.parametrize("vectorize", [False, True])
 def test_reference_reduce_queries_compile(vectorize):
     st2 = rq.students_table(2)
