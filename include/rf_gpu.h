@@ -162,10 +162,12 @@ int rf_plan_launch(rf_plan* plan, const rf_arg* args, int32_t n_args, void* dev_
  * variable RF_NOALLOC_LIMIT, in bytes, lowers that limit; it cannot raise it).  Value-output
  * (Reduce) plans only, and every table a plan probes must already have its index
  * (rf_table_build_index), since building one allocates.  `host_out` receives the result, as in
- * rf_plan_run; the call waits for it.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current.  All calls share the array, which
- * keeps the last call's contents: calls that overlap on the GPU (other threads or streams)
- * race and must be serialised by the caller.
+ * rf_plan_run, and is left untouched when the run fails; the call waits for it.  The array is
+ * set up by rf_gpu_init: it loads the module that holds the array and looks up its device
+ * address (cudaGetSymbolAddress) with the device current, so no run does either.  All calls
+ * share the array, which keeps the last call's contents (each run clears what must start at
+ * zero): calls that overlap on the GPU (other threads or streams) race and must be serialised
+ * by the caller.
  * No counterpart in the reference (its generated code runs on the host). */
 int rf_plan_run_noalloc(rf_plan* plan, const rf_arg* args, int32_t n_args, void* host_out, void* stream);
 /* A host function with the signature of the reference's generated query function:

@@ -367,6 +367,19 @@ extern "C" int rf_gpu_init(int device, rf_ctx** out)
     cudaDeviceGetAttribute(&ctx->pageable_direct, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
     CUDA_TRY(nullptr, cudaMalloc((void**)&ctx->dev_err, sizeof(int)));
     CUDA_TRY(nullptr, cudaMemset(ctx->dev_err, 0, sizeof(int)));
+    // rf_plan_run_noalloc's fixed array: with lazy module loading the array's device memory is
+    // set up when its module first loads, so the address is looked up here (loading the module
+    // while the caller may still allocate), never inside a run that promises no allocation
+    {
+        void* scratch = nullptr;
+        size_t scratch_bytes = 0;
+        int e = rf_k_noalloc_scratch(device, &scratch, &scratch_bytes);
+        if (e) {
+            cudaFree(ctx->dev_err);
+            cudaStreamDestroy(ctx->stream);
+            return RF_ERR_CUDA;
+        }
+    }
     *out = ctx.release();
     return RF_OK;
 }
@@ -2082,9 +2095,12 @@ extern "C" int rf_plan_run_noalloc(rf_plan* p, const rf_arg* args, int32_t n_arg
     if (rc) return rc;
     long long ntiles = (hi - lo + P.tile_rows - 1) / P.tile_rows;
     int units = units_for(p, ntiles);
-    // layout: [counter 256][loop bounds 256][result, 256-aligned][partials: units x acc_bytes]
+    // layout: [counter 256][loop bounds 256][error word at 752][result at 768, 256-aligned]
+    // [partials: units x max(acc_bytes, 8); every unit writes at least one 8-byte accumulator]
+    const size_t err_at = 752, out_at = 768;
     size_t out_bytes = (pl.out_size + 255) / 256 * 256;
-    size_t need = 512 + out_bytes + (size_t)units * pl.acc_bytes;
+    size_t acc = pl.acc_bytes ? pl.acc_bytes : 8;
+    size_t need = out_at + out_bytes + (size_t)units * acc;
     if (need > cap)
         return fail(ctx, RF_ERR_INVALID,
                     "rf_plan_run_noalloc: this run needs %zu bytes of scratch, the fixed array holds %zu "
@@ -2092,8 +2108,8 @@ extern "C" int rf_plan_run_noalloc(rf_plan* p, const rf_arg* args, int32_t n_arg
     unsigned char* b = (unsigned char*)base;
     P.counter = (unsigned int*)b;
     P.range = pl.device_range ? (long long*)(b + 256) : nullptr;
-    P.out = b + 512;
-    P.partials = b + 512 + out_bytes;
+    P.out = b + out_at;
+    P.partials = b + out_at + out_bytes;
     P.nunits = units;
     // the last-unit-done merge counts arrivals from zero
     CUDA_TRY(ctx, cudaMemsetAsync(P.counter, 0, sizeof(unsigned int), s));
@@ -2106,9 +2122,24 @@ extern "C" int rf_plan_run_noalloc(rf_plan* p, const rf_arg* args, int32_t n_arg
                        : units;
         if ((rc = launch(ctx, p->fns[i], grid, k.threads, k.smem, s, &P))) return rc;
     }
-    CUDA_TRY(ctx, cudaMemcpyAsync(host_out, P.out, pl.out_size, cudaMemcpyDeviceToHost, s));
+    // the error word is placed just before the result, so one copy brings back both; the result
+    // reaches host_out only once the error word says the run succeeded (as in rf_plan_run)
+    CUDA_TRY(ctx, cudaMemcpyAsync(b + err_at, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToDevice, s));
+    unsigned char small[16 + 4096];
+    const bool one_copy = pl.out_size <= sizeof(small) - 16;
+    const size_t back = one_copy ? 16 + pl.out_size : 16;
+    CUDA_TRY(ctx, cudaMemcpyAsync(small, b + err_at, back, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(ctx, cudaStreamSynchronize(s));
-    return check_device_error(ctx);
+    int err;
+    memcpy(&err, small, sizeof(int));
+    if ((rc = device_error(ctx, err))) return rc;
+    if (one_copy) {
+        memcpy(host_out, small + 16, pl.out_size);
+    } else {  // a result larger than the stack buffer: a second copy, after the check
+        CUDA_TRY(ctx, cudaMemcpyAsync(host_out, P.out, pl.out_size, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    }
+    return RF_OK;
 }
 
 extern "C" int rf_plan_run(rf_plan* p, const rf_arg* args, int32_t n_args, void* out, void* stream)
