@@ -13,11 +13,16 @@ GB/s = algorithmic bytes (each referenced column read once) / time.
              copies of the referenced columns and the device->host result copy inside the timing
   roofline   achieved algorithmic GB/s of the main kernel against the measured HBM copy peak
   cpu_baseline  the oracle (Reffine's CPU loop restated, g++ -O3, one core) on the same table
+  parity     the GPU result against the oracle's on the same full-size tables: integers
+             bit-exact, FP64 max relative error (the bar is 1e-12)
+  per_config the same measurements (value, roofline, e2e, cpu_baseline, parity) for the other
+             three configurations: filter+sum 6M, hash group-by 100M Zipf, join 10M x 200M
   serving    10k requests over resident tables of log-uniform size, Poisson arrivals: the
              continuous-batching server against per-query launches on the same GPU (p50/p99
              latency, queries/s, GB/s), every result checked against the query run alone
 
---impl reference times the oracle port alone (the reference's CPU path; it is single-threaded).
+--impl reference times the oracle port alone (the reference's CPU path; it is single-threaded);
+it counts bytes from the columns each workload declares and loads nothing of the GPU backend.
 Multi-GPU (torchrun): each rank scans its own partition (weak scaling), no collective on the
 data path; rank 0 prints the max-over-ranks time.
 """
@@ -141,43 +146,46 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
-def build_workload(config: int, rank: int, world: int, rows: int = 0):
-    """Returns (name, tables list, query Func, rows, config dict).  Each rank gets its own
-    partition (a different seed), so per-GPU work is fixed as N grows."""
+class Workload:
+    """One benchmark configuration: seeded tables, the query, and the columns it reads (declared
+    here, so the CPU arm counts algorithmic bytes without the GPU library)."""
+
+    def __init__(self, name, tables, fn, rows, cfg, cols):
+        self.name, self.tables, self.fn, self.rows, self.cfg, self.cols = name, tables, fn, rows, cfg, cols
+
+    def algorithmic_bytes(self) -> int:
+        return sum(t.nbytes(c) for t, c in zip(self.tables, self.cols))
+
+
+WORKLOAD_NAMES = {0: "filter_sum_6M", 1: "groupby_6groups_60M", 2: "hash_groupby_zipf1.1_100M", 3: "join_10M_x_200M"}
+
+
+def build_workload(config: int, rank: int, world: int, rows: int = 0) -> Workload:
+    """Each rank gets its own partition (a different seed), so per-GPU work is fixed as N grows."""
     from reffine_gb300 import workloads as W
     seed_off = 1000 * rank
+    name = WORKLOAD_NAMES.get(config)
     if config == 0:
         n = rows or 6_000_000
         t = W.filter_sum_table(n, seed=0 + seed_off)
-        return ("filter_sum_6M", [t], W.filter_sum_query(t.get_data_type()), n,
-                {"rows": n, "query": "SUM(price*discount), COUNT over day in [730,1095), discount in [0.05,0.07], "
-                                     "quantity < 24"})
+        return Workload(name, [t], W.filter_sum_query(t.get_data_type()), n, build_cfg(0, n), [[1, 2, 3, 4]])
     if config == 1:
         n = rows or 60_000_000
         t = W.groupby_table(n, seed=1 + seed_off)
-        return ("groupby_6groups_60M", [t], W.groupby_query(t.get_data_type()), n,
-                {"rows": n, "groups": 6, "query": "per (flag_a, flag_b): SUM qty/price/disc_price/charge, AVG "
-                                                  "qty/price/disc, COUNT over day <= 2450"})
+        return Workload(name, [t], W.groupby_query(t.get_data_type()), n, build_cfg(1, n), [[1, 2, 3, 4, 5, 6, 7]])
     if config == 2:
         n, nd = rows or 100_000_000, 10_000_000
         t = W.hashgroup_table(n, min(nd, n), 1.1, seed=2 + seed_off)
-        return ("hash_groupby_zipf1.1_100M", [t], W.hashgroup_query(t.get_data_type()), n,
-                {"rows": n, "distinct_ranks": nd, "zipf_s": 1.1,
-                 "query": "per key: SUM(value) f64, COUNT i64 (unsorted int64 keys; hash table at load 0.5)"})
+        return Workload(name, [t], W.hashgroup_query(t.get_data_type()), n, build_cfg(2, n), [[0, 1]])
     if config == 3:
         nb, npr = 10_000_000, rows or 200_000_000
         b, p = W.join_tables(nb, npr, seed=3 + seed_off)
-        return ("join_10M_x_200M", [b, p], W.join_query(b.get_data_type(), p.get_data_type()), npr,
-                {"rows": npr, "build_rows": nb, "query": "SUM(amount), COUNT per build attr < 5, probe day in [0,365)"})
+        return Workload(name, [b, p], W.join_query(b.get_data_type(), p.get_data_type()), npr, build_cfg(3, npr),
+                        [[0, 1], [1, 2, 3]])
     raise SystemExit("config %d is not benchmarked by this script" % config)
 
 
-def referenced_bytes(plan, tables) -> int:
-    from reffine_gb300.ir import DataType
-    tot = 0
-    for i, t in enumerate(tables):
-        tot += int(plan.info.bytes_per_row[i]) * len(t)
-    return tot
+L2_NOTE = "inputs larger than L2 (129 MB); no flush between steps"
 
 
 def reference_form(config, fn, tables):
@@ -190,66 +198,304 @@ def reference_form(config, fn, tables):
     return W.hashgroup_query(ree.get_data_type()), [ree]
 
 
-def cpu_baseline(fn, tables, nbytes, budget_s=20.0, note=""):
-    """The oracle port (serial C++ loop, one core) on the same tables."""
+def oracle_run(fn, tables, nbytes, budget_s=20.0, note=""):
+    """The oracle port (Reffine's serial loop restated, g++ -O3, one core) on the same tables:
+    (cpu_baseline dict, seconds per run, the result of the first run)."""
     from oracle import loopgen
     q = loopgen.Query(fn)
-    out, cargs = q.prepare(*tables)
-    times = []
+    table_out = fn.output.type.is_vector()
+    times, result = [], None
     t_end = time.perf_counter() + budget_s
     while len(times) < 5 and (not times or time.perf_counter() + times[-1] < t_end):
+        out, cargs = q.prepare(*tables)
         t0 = time.perf_counter()
         q.run_prepared(out, cargs)
         times.append(time.perf_counter() - t0)
+        r = q.result(out)  # frees a table result's buffers
+        if result is None:
+            result = r
     sec = float(np.median(times))
-    return {"value": nbytes / sec / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
-            "sample": "the full table, %d run(s), median %.3f s; %s%s" % (len(times), sec, platform.processor() or
-                                                                          platform.machine(), note)}, sec
+    kind = platform.processor() or platform.machine()
+    return ({"value": nbytes / sec / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+             "sample": "the full table, %d run(s), median %.3f s; %s%s" % (len(times), sec, kind, note)},
+            sec, result)
+
+
+def _flatten(v):
+    if isinstance(v, (tuple, list)):
+        for x in v:
+            yield from _flatten(x)
+    else:
+        yield v
+
+
+def value_parity(got, ref) -> dict:
+    """Integers bit-exact, FP64 relative error against the oracle (1e-12 is the bar)."""
+    import math
+    g, r = list(_flatten(got)), list(_flatten(ref))
+    if len(g) != len(r):
+        return {"int_exact": False, "max_rel_err": None, "fields": [len(g), len(r)], "ok": False}
+    int_ok, rel = True, 0.0
+    for a, b in zip(g, r):
+        if isinstance(b, float):
+            if math.isnan(b) or math.isinf(b):
+                same = (math.isnan(a) and math.isnan(b)) or a == b
+                rel = rel if same else math.inf
+            else:
+                rel = max(rel, abs(a - b) / max(abs(b), 1e-300))
+        else:
+            int_ok &= a == b
+    return {"int_exact": bool(int_ok), "max_rel_err": rel, "fields": len(r), "ok": bool(int_ok and rel <= 1e-12)}
+
+
+def table_parity(out, ref, values=None, keys=None) -> dict:
+    """A table result against the oracle's: rows canonicalised by column 0 (the key); integer
+    columns bit-exact, FP64 columns by relative error.  With the input key/value columns given,
+    also the distance of both sums from exact sums (math.fsum) for the 8 largest groups."""
+    import math
+    order = np.argsort(out["cols"][0], kind="stable")
+    cols = [c[order] for c in out["cols"]]
+    res = {"rows": int(out["len"]), "oracle_rows": int(ref["len"])}
+    if out["len"] != ref["len"]:
+        res.update(int_exact=False, max_rel_err=None, ok=False)
+        return res
+    int_ok, rel = True, 0.0
+    for g, r in zip(cols, ref["cols"]):
+        if np.issubdtype(r.dtype, np.floating):
+            den = np.maximum(np.abs(r), 1e-300)
+            rel = max(rel, float(np.max(np.abs(g - r) / den)) if len(r) else 0.0)
+        else:
+            int_ok &= bool(np.array_equal(g, r))
+    res.update(int_exact=int_ok, max_rel_err=rel, ok=bool(int_ok and rel <= 1e-12))
+    if keys is not None and len(ref["cols"]) >= 3 and len(ref["cols"][2]):
+        top = np.argsort(ref["cols"][2])[-8:]
+        worst_gpu = worst_cpu = 0.0
+        for i in top:
+            k = ref["cols"][0][i]
+            exact = math.fsum(values[keys == k].tolist())
+            if exact:
+                worst_gpu = max(worst_gpu, abs(cols[1][i] - exact) / abs(exact))
+                worst_cpu = max(worst_cpu, abs(ref["cols"][1][i] - exact) / abs(exact))
+        res["largest_groups_vs_exact_sum"] = {"groups": len(top), "rows_in_largest": int(ref["cols"][2][top[-1]]),
+                                              "gpu_max_rel_err": worst_gpu, "oracle_max_rel_err": worst_cpu}
+    return res
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU path for the same workload: the oracle port of Reffine's generated
+    serial loop, one core (the reference's generated code is single-threaded).  Counts bytes from
+    the workload's declared columns; loads nothing of the GPU backend."""
     if rank != 0:
         return 0
-    name, tables, fn, rows, cfg = build_workload(args.config, 0, 1, args.rows)
-    from reffine_gb300 import engine
-    # algorithmic bytes come from the lowering's column analysis (no GPU needed for it)
+    wl = build_workload(args.config, 0, 1, args.rows)
+    nbytes = wl.algorithmic_bytes()
+    fn, tables = reference_form(args.config, wl.fn, wl.tables)
     from oracle import loopgen
-    nbytes = sum(t.nbytes(_cols_read_cpu(fn, i)) for i, t in enumerate(tables))
-    fn, tables = reference_form(args.config, fn, tables)
     q = loopgen.Query(fn)
-    out, cargs = q.prepare(*tables)
-    for _ in range(args.warmup):
-        q.run_prepared(out, cargs)
-    times = []
-    for _ in range(args.steps):
+    table_out = fn.output.type.is_vector()
+
+    def once():
+        out, cargs = q.prepare(*tables)
         t0 = time.perf_counter()
         q.run_prepared(out, cargs)
-        times.append(time.perf_counter() - t0)
+        dt = time.perf_counter() - t0
+        if table_out:
+            q.result(out)
+        return dt
+
+    for _ in range(args.warmup):
+        once()
+    times = [once() for _ in range(args.steps)]
     sec = float(np.mean(times))
     val = nbytes / sec / 1e9
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": name, **cfg, "l2": "inputs larger than L2"},
+            "config": {"workload": wl.name, **wl.cfg, "l2": L2_NOTE},
             "cpu_baseline": {"value": val, "unit": "GB/s", "cores": 1, "kind": "port",
-                             "sample": "the full table per step (Reffine's serial loop restated, g++ -O3)"},
-            "e2e": {"value": val, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": "the full table per step (Reffine's serial loop restated, g++ -O3, "
+                                       "one core)"},
+            "e2e": {"value": val, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "algorithmic_bytes_per_step": nbytes}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def _cols_read_cpu(fn, input_idx):
-    """Referenced columns of a Func input, from the lowering (rf_plan_check's source)."""
-    import re
-    from reffine_gb300 import engine
-    src = engine.check(fn)
-    slot = 0
-    for i, s in enumerate(fn.inputs):
-        if i == input_idx:
-            break
-        if s.type.is_vector():
-            slot += 1
-    return sorted({int(c) for c in re.findall(r"P\.t\[%d\]\.col\[(\d+)\]" % slot, src)})
+def _pinned_copy(eng, tables):
+    from reffine_gb300.table import Column, Table
+    pinned, ptables = [], []
+    for t in tables:
+        cols = []
+        for c in t.columns:
+            buf = eng.host_alloc(c.data.nbytes)
+            v = buf.view(c.data.dtype, len(c.data))
+            v[:] = c.data
+            pinned.append(buf)
+            cols.append(Column(c.name, c.dtype, v, c.valid, c.run_ends))
+        ptables.append(Table(t.name, t.dim, cols))
+    return pinned, ptables
+
+
+def measure_config(eng, wl: Workload, config: int, args, rank: int, world: int, dist, cpu: bool,
+                   pageable: bool = True) -> dict:
+    """Times one workload: kernel throughput (tables resident, CUDA events on the launch stream),
+    the roofline of its main kernel, end to end through the reference-shaped host call, the CPU
+    baseline and full-size parity against the oracle."""
+    from reffine_gb300 import cudart, engine
+    dts = [eng.upload(t) for t in wl.tables]
+    plan = eng.compile(wl.fn)
+    nbytes = sum(int(plan.info.bytes_per_row[i]) * len(t) for i, t in enumerate(wl.tables))
+    declared = wl.algorithmic_bytes()
+    pargs = plan.args(*dts)
+    n = len(dts)
+    stream = eng.stream
+    table_out = bool(plan.info.output_is_table)
+    out_rows = [0]
+    last = [None]
+    tuning = {}
+    # the autotuner picks the scan tile (or the hash table's sizing) for this shape and size
+    # once, before warm-up (rf_plan_tune; every later run of the shape uses it)
+    if not table_out and plan.kind in (1, 2):
+        tuning["tile_rows"], _ = plan.tune(*dts, reps=3)
+    elif plan.kind == 5:
+        tuning["hash_slots_per_100_keys"], _ = plan.tune(*dts, reps=2)
+
+    def step(keep=False):
+        if not table_out:
+            plan.launch(pargs, n)
+            return
+        import ctypes
+        h = ctypes.c_void_p()
+        eng.check(eng.lib.rf_plan_run(plan.h, pargs, n, ctypes.byref(h), None))
+        r = ctypes.c_int64()
+        eng.lib.rf_table_num_rows(h, ctypes.byref(r))
+        out_rows[0] = r.value
+        if keep:
+            dtab = engine.DeviceTable(eng, h, None, [])
+            last[0] = dtab.export()
+            dtab.h = None  # freed below
+        eng.lib.rf_table_free(h)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    eng.sync()
+    out_bytes = 0
+    if table_out:  # output bytes join the algorithmic bytes (rows x output row size)
+        out_bytes = out_rows[0] * sum(d.size() for d in wl.fn.output.type.dtypes)
+        nbytes += out_bytes
+        declared += out_bytes
+
+    evs = [cudart.Event() for _ in range(args.steps + 1)]
+    clocks = ClockSampler(eng.device)
+    clocks.start()
+    dist.barrier()
+    eng.sync()
+    l0 = eng.launch_count()
+    evs[0].record(stream)
+    for k in range(args.steps):
+        step()
+        evs[k + 1].record(stream)
+    eng.sync()
+    dist.barrier()
+    l1 = eng.launch_count()
+    clk = clocks.stop()
+    per = [evs[k].elapsed_ms(evs[k + 1]) for k in range(args.steps)]
+    total_ms = dist.max(sum(per))
+    ms_step = total_ms / args.steps
+    all_bytes = dist.sum(nbytes)
+    value = all_bytes / (ms_step / 1e3) / 1e9
+
+    # the result (outside the timing), for parity
+    if table_out:
+        step(keep=True)
+        got = last[0]
+    else:
+        out = plan.new_out()
+        plan.run_args(pargs, n, out)
+        got = engine.from_c(out)
+
+    peak, peak_kind = peak_hbm()
+    kern_ms = float(np.mean(per))
+    achieved = nbytes / (kern_ms / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(wl.name)
+        except Exception:
+            traffic = None
+
+    # end to end through the reference-shaped call (compile_op's function pointer): host
+    # tables in pinned memory, host->device copies of the referenced columns and the result's
+    # copy back inside the timing
+    h2d = sum(int(plan.info.bytes_per_row[i]) * len(t) for i, t in enumerate(wl.tables))
+    d2h = out_bytes if table_out else int(plan.info.output_size)
+    e2e = {"value": None, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    pinned = []
+    try:
+        if args.e2e_steps <= 0:
+            raise RuntimeError("e2e skipped (--e2e-steps 0)")
+        pinned, ptables = _pinned_copy(eng, wl.tables)
+        q = engine.compile_op(wl.fn, engine=eng)
+        q(*ptables)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            q(*ptables)
+        e2e_s = dist.max(time.perf_counter() - t0) / args.e2e_steps
+        e2e.update(value=all_bytes / e2e_s / 1e9, ms_per_step=e2e_s * 1e3,
+                   path="compile_op function pointer (rf_plan_thunk), pinned host tables" +
+                        ("; the result table exported to host Arrow memory" if table_out else ""))
+        if pageable and not table_out:
+            # the same call on the tables' own (pageable, numpy) memory, as a caller's ArrowTable2
+            # holds it
+            q(*wl.tables)
+            dist.barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                q(*wl.tables)
+            pg_s = dist.max(time.perf_counter() - t0) / args.e2e_steps
+            e2e["pageable"] = {"value": all_bytes / pg_s / 1e9, "ms_per_step": pg_s * 1e3}
+        q.plan.free()
+        del ptables
+    except Exception as ex:  # report, do not hide
+        e2e["error"] = str(ex)[:300]
+    finally:
+        for b in pinned:
+            b.free()
+
+    res = {"workload": wl.name, "value": value, "unit": "GB/s", "ms_per_step": ms_step, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "rows_per_s": wl.rows * world / (ms_step / 1e3),
+           "bytes_per_step": nbytes, "tuning": tuning or None,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                        "kernel": {1: "rf_main (scan-reduce)", 2: "rf_main (grouped scan-reduce)",
+                                   5: "rf_hg_agg + materialisation (hash group-by)"}.get(plan.kind, str(plan.kind)),
+                        "algorithmic_bytes_per_launch": nbytes},
+           "e2e": e2e, "gpu_launches": int(l1 - l0), "clocks": clk}
+    if nbytes != declared:
+        res["bytes_mismatch"] = {"plan": nbytes, "declared": declared}
+
+    if cpu and rank == 0:
+        rfn, rtabs = reference_form(config, wl.fn, wl.tables)
+        base, _, ref = oracle_run(rfn, rtabs, nbytes, note="" if config != 2 else
+                                  "; keys pre-sorted and run-end encoded (the reference's grouped form), sort not "
+                                  "timed")
+        res["cpu_baseline"] = base
+        if table_out:
+            res["parity"] = table_parity(got, ref, values=wl.tables[0].columns[1].data,
+                                         keys=wl.tables[0].columns[0].data)
+        else:
+            res["parity"] = value_parity(got, ref)
+        res["parity"]["against"] = "oracle on the same full-size tables (rows %d)" % wl.rows
+    else:
+        res["cpu_baseline"] = None
+        res["parity"] = None
+    res["result_sample"] = ("%d output rows" % out_rows[0]) if table_out else str(got)[:200]
+    for d in dts:
+        d.free()
+    plan.free()
+    return res
 
 
 def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5), table_lanes: int = 0,
@@ -336,7 +582,8 @@ def bench_ingest(eng, config: int, rows: int = 0, reps: int = 3):
     import tempfile
     from reffine_gb300.ipc_write import write_ipc
     from reffine_gb300.table import read_ipc_c, release_c
-    name, tables, fn, nrows, cfg = build_workload(config, 0, 1, rows)
+    wl = build_workload(config, 0, 1, rows)
+    name, tables, fn, nrows = wl.name, wl.tables, wl.fn, wl.rows
     if len(tables) != 1:
         raise ValueError("ingest is measured on single-table configurations (0, 1, 2)")
     t = tables[0]
@@ -406,6 +653,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--rows", type=int, default=0, help="override the row count (profiling a smaller case)")
+    ap.add_argument("--per-config", default="auto",
+                    help="comma-separated further configurations measured after the headline one and reported "
+                         "under per_config ('auto': the other three of 0-3 when the headline is config 1 at "
+                         "full size on one GPU; 'none')")
     ap.add_argument("--serving-queries", type=int, default=10_000,
                     help="requests of the batched-serving comparison (0: skip it)")
     ap.add_argument("--serving-max-rows", type=int, default=50_000_000)
@@ -437,132 +688,29 @@ def main():
         eng.close()
         return 0
 
-    from reffine_gb300 import cudart, engine
+    from reffine_gb300 import engine
     dist = Dist(world)
     eng = engine.Engine(local)
-    name, tables, fn, rows, cfg = build_workload(args.config, rank, world, args.rows)
-    dts = [eng.upload(t) for t in tables]
-    plan = eng.compile(fn)
-    nbytes = referenced_bytes(plan, tables)
-    pargs = plan.args(*dts)
-    n = len(dts)
-    stream = eng.stream
-    out_check = None if plan.info.output_is_table else plan.new_out()
+    wl = build_workload(args.config, rank, world, args.rows)
+    head = measure_config(eng, wl, args.config, args, rank, world, dist, cpu=not args.no_cpu)
+    del wl
 
-    table_out = bool(plan.info.output_is_table)
-    out_rows = [0]
-    # the tiling autotuner picks the scan tile for this shape and size once, before warm-up
-    # (rf_plan_tune; every later run of the shape uses it)
-    tile_rows = hash_slots = None
-    if not table_out and plan.kind in (1, 2):
-        tile_rows, _ = plan.tune(*dts, reps=3)
-    elif plan.kind == 5:  # hash group-by: the table's slots per 100 distinct keys
-        hash_slots, _ = plan.tune(*dts, reps=2)
-
-    def step():
-        if not table_out:
-            plan.launch(pargs, n)
-            return
-        import ctypes
-        h = ctypes.c_void_p()
-        eng.check(eng.lib.rf_plan_run(plan.h, pargs, n, ctypes.byref(h), None))
-        r = ctypes.c_int64()
-        eng.lib.rf_table_num_rows(h, ctypes.byref(r))
-        out_rows[0] = r.value
-        eng.lib.rf_table_free(h)
-
-    for _ in range(max(args.warmup, 3)):
-        step()
-    eng.sync()
-    if table_out:  # output bytes join the algorithmic bytes (rows x output row size)
-        nbytes += out_rows[0] * sum(d.size() for d in fn.output.type.dtypes)
-
-    evs = [cudart.Event() for _ in range(args.steps + 1)]
-    clocks = ClockSampler(local)
-    clocks.start()
-    dist.barrier()
-    eng.sync()
-    l0 = eng.launch_count()
-    evs[0].record(stream)
-    for k in range(args.steps):
-        step()
-        evs[k + 1].record(stream)
-    eng.sync()
-    dist.barrier()
-    l1 = eng.launch_count()
-    clk = clocks.stop()
-    per = [evs[k].elapsed_ms(evs[k + 1]) for k in range(args.steps)]
-    total_ms = dist.max(sum(per))
-    ms_step = total_ms / args.steps
-    all_bytes = dist.sum(nbytes)
-    value = all_bytes / (ms_step / 1e3) / 1e9
-    if not table_out:
-        plan.run_args(pargs, n, out_check)  # result of the last configuration, for the log
-
-    # kernel roofline (this rank): algorithmic bytes per launch / mean launch time
-    peak, peak_kind = peak_hbm()
-    kern_ms = float(np.mean(per))
-    achieved = nbytes / (kern_ms / 1e3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
+    if args.per_config == "auto":
+        others = [c for c in (0, 1, 2, 3) if c != args.config] if (args.config == 1 and not args.rows and world == 1) \
+            else []
+    elif args.per_config in ("", "none"):
+        others = []
+    else:
+        others = [int(c) for c in args.per_config.split(",") if c.strip() and int(c) != args.config]
+    per_config = {}
+    for c in others:
         try:
-            traffic = json.load(open(tf)).get(name)
-        except Exception:
-            traffic = None
-
-    # end to end through the reference-shaped call: host tables in pinned memory
-    e2e = None
-    if args.e2e_steps <= 0:
-        args.e2e_steps = 0
-    h2d = sum(int(plan.info.bytes_per_row[i]) * len(t) for i, t in enumerate(tables))
-    try:
-        if not args.e2e_steps:
-            raise RuntimeError("e2e skipped (--e2e-steps 0)")
-        from reffine_gb300.table import Column, Table
-        pinned = []
-        ptables = []
-        for t in tables:
-            cols = []
-            for c in t.columns:
-                buf = eng.host_alloc(c.data.nbytes)
-                v = buf.view(c.data.dtype, len(c.data))
-                v[:] = c.data
-                pinned.append(buf)
-                cols.append(Column(c.name, c.dtype, v, c.valid, c.run_ends))
-            ptables.append(Table(t.name, t.dim, cols))
-        if table_out:
-            raise RuntimeError("e2e for table outputs is measured by the serving benchmark")
-        q = engine.compile_op(fn, engine=eng)
-        q(*ptables)
-        dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            q(*ptables)
-        e2e_s = dist.max(time.perf_counter() - t0) / args.e2e_steps
-        e2e = {"value": all_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": int(plan.info.output_size), "ms_per_step": e2e_s * 1e3,
-               "path": "compile_op function pointer (rf_plan_thunk), pinned host tables"}
-        # the same call on the tables' own (pageable, numpy) memory, as a caller's ArrowTable2 holds it
-        q(*tables)
-        dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            q(*tables)
-        pg_s = dist.max(time.perf_counter() - t0) / args.e2e_steps
-        e2e["pageable"] = {"value": all_bytes / pg_s / 1e9, "ms_per_step": pg_s * 1e3}
-        del ptables
-        for b in pinned:
-            b.free()
-    except Exception as ex:  # report, do not hide
-        e2e = {"value": None, "unit": "GB/s", "error": str(ex)[:300], "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": int(plan.info.output_size)}
-
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        rfn, rtabs = reference_form(args.config, fn, tables)
-        cpu, _ = cpu_baseline(rfn, rtabs, nbytes, note="" if args.config != 2 else
-                              "; keys pre-sorted and run-end encoded (the reference's grouped form), sort not timed")
+            w = build_workload(c, rank, world, 0)
+            per_config[WORKLOAD_NAMES[c]] = measure_config(eng, w, c, args, rank, world, dist, cpu=not args.no_cpu,
+                                                           pageable=False)
+            del w
+        except Exception as ex:  # one configuration's failure is reported, not fatal to the line
+            per_config[WORKLOAD_NAMES.get(c, str(c))] = {"error": "%s: %s" % (type(ex).__name__, str(ex)[:400])}
 
     serving = None
     if rank == 0 and args.serving_queries > 0 and world == 1:
@@ -570,23 +718,34 @@ def main():
                                    args.serving_table_priority)
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-                "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": name, **cfg, "bytes_per_step": nbytes, "l2": "inputs larger than L2 (no flush)",
-                           "tile_rows": tile_rows, "hash_slots_per_100_keys": hash_slots,
-                           "tuning_from": "autotuner (rf_plan_tune) before warm-up"},
-                "rows_per_s": rows * world / (ms_step / 1e3),
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                             "kernel": {1: "rf_main (scan-reduce)", 2: "rf_main (grouped scan-reduce)",
-                                        5: "rf_hg_agg + materialisation (hash group-by)"}.get(plan.kind, str(plan.kind)),
-                             "algorithmic_bytes_per_launch": nbytes},
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(l1 - l0), "clocks": clk, "serving": serving,
-                "result_sample": ("%d output rows" % out_rows[0]) if table_out else str(engine.from_c(out_check))[:200]}
+        line = {"metric": METRIC, "value": head["value"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": head["workload"], **build_cfg(args.config, args.rows), "l2": L2_NOTE},
+                "tuning": dict(head["tuning"] or {}, source="autotuner (rf_plan_tune) before warm-up"),
+                "bytes_per_step": head["bytes_per_step"], "rows_per_s": head["rows_per_s"],
+                "roofline": head["roofline"], "cpu_baseline": head["cpu_baseline"], "e2e": head["e2e"],
+                "parity": head["parity"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
+                "per_config": per_config or None, "serving": serving, "result_sample": head["result_sample"]}
+        if "bytes_mismatch" in head:
+            line["bytes_mismatch"] = head["bytes_mismatch"]
         print(json.dumps(line), flush=True)
     eng.close()
     return 0
+
+
+def build_cfg(config: int, rows: int) -> dict:
+    """The config dict of a workload without building its tables (both arms print the same)."""
+    cfgs = {0: lambda n: {"rows": n, "query": "SUM(price*discount), COUNT over day in [730,1095), discount in "
+                                               "[0.05,0.07], quantity < 24"},
+            1: lambda n: {"rows": n, "groups": 6, "query": "per (flag_a, flag_b): SUM qty/price/disc_price/charge, "
+                                                           "AVG qty/price/disc, COUNT over day <= 2450"},
+            2: lambda n: {"rows": n, "distinct_ranks": min(10_000_000, n), "zipf_s": 1.1,
+                          "query": "per key: SUM(value) f64, COUNT i64 (unsorted int64 keys; hash table at load 0.5)"},
+            3: lambda n: {"rows": n, "build_rows": 10_000_000,
+                          "query": "SUM(amount), COUNT per build attr < 5, probe day in [0,365)"}}
+    default = {0: 6_000_000, 1: 60_000_000, 2: 100_000_000, 3: 200_000_000}
+    return cfgs[config](rows or default[config])
 
 
 if __name__ == "__main__":

@@ -206,29 +206,7 @@ class DeviceTable:
         s, a = ArrowSchema(), ArrowArray()
         self.eng.check(self.eng.lib.rf_table_export(self.h, ctypes.byref(s), ctypes.byref(a)))
         try:
-            cols, valids = [], []
-            for c in range(a.n_children):
-                cs, ca = s.children[c].contents, a.children[c].contents
-                fmt = cs.format.decode()
-                arr = ca
-                if fmt == "+r":
-                    arr = ca.children[1].contents
-                    fmt = cs.children[1].contents.format.decode()
-                dt = {"c": np.int8, "C": np.uint8, "s": np.int16, "S": np.uint16, "i": np.int32, "I": np.uint32,
-                      "l": np.int64, "L": np.uint64, "f": np.float32, "g": np.float64}[fmt]
-                n = arr.length
-                vals = np.zeros(n, dtype=dt)
-                if n and arr.buffers[1]:
-                    ctypes.memmove(vals.ctypes.data, arr.buffers[1], n * vals.itemsize)
-                cols.append(vals)
-                if arr.buffers[0]:
-                    nb = (n + 15) // 16 * 2
-                    bm = np.zeros(nb, dtype=np.uint8)
-                    ctypes.memmove(bm.ctypes.data, arr.buffers[0], nb)
-                    valids.append(unpack_validity(bm, n))
-                else:
-                    valids.append(None)
-            return {"cols": cols, "valid": valids, "len": a.length}
+            return arrow_to_dict(s, a)
         finally:
             rel_a = ctypes.CFUNCTYPE(None, ctypes.POINTER(ArrowArray))(a.release) if a.release else None
             rel_s = ctypes.CFUNCTYPE(None, ctypes.POINTER(ArrowSchema))(s.release) if s.release else None
@@ -236,6 +214,34 @@ class DeviceTable:
                 rel_a(ctypes.byref(a))
             if rel_s:
                 rel_s(ctypes.byref(s))
+
+
+def arrow_to_dict(s: ArrowSchema, a: ArrowArray) -> Dict:
+    """Copies an Arrow struct batch (a table's columns as children) into numpy arrays:
+    {"cols": [numpy...], "valid": [bool mask or None...], "len"}."""
+    cols, valids = [], []
+    for c in range(a.n_children):
+        cs, ca = s.children[c].contents, a.children[c].contents
+        fmt = cs.format.decode()
+        arr = ca
+        if fmt == "+r":
+            arr = ca.children[1].contents
+            fmt = cs.children[1].contents.format.decode()
+        dt = {"c": np.int8, "C": np.uint8, "s": np.int16, "S": np.uint16, "i": np.int32, "I": np.uint32,
+              "l": np.int64, "L": np.uint64, "f": np.float32, "g": np.float64}[fmt]
+        n = arr.length
+        vals = np.zeros(n, dtype=dt)
+        if n and arr.buffers[1]:
+            ctypes.memmove(vals.ctypes.data, arr.buffers[1], n * vals.itemsize)
+        cols.append(vals)
+        if arr.buffers[0]:
+            nb = (n + 15) // 16 * 2
+            bm = np.zeros(nb, dtype=np.uint8)
+            ctypes.memmove(bm.ctypes.data, arr.buffers[0], nb)
+            valids.append(unpack_validity(bm, n))
+        else:
+            valids.append(None)
+    return {"cols": cols, "valid": valids, "len": a.length}
 
 
 class Plan:
@@ -396,8 +402,12 @@ def compile_op(fn: ir.Func, vectorize: bool = False, engine: Optional[Engine] = 
             argtypes.append(_CT[s.type.btype])
     cfn = ctypes.CFUNCTYPE(None, *argtypes)(addr)
 
+    table_out = bool(plan.info.output_is_table)
+
     def call(*inputs):
-        out = plan.new_out()
+        # a table result comes back as an ArrowTable* that the plan keeps (as the reference's
+        # memman keeps its outputs, src/engine/memory.cpp:11-16)
+        out = ctypes.c_void_p() if table_out else plan.new_out()
         cargs = [ctypes.cast(ctypes.byref(out), ctypes.c_void_p)]
         keep = []
         for s, v in zip(fn.inputs, inputs):
@@ -408,6 +418,11 @@ def compile_op(fn: ir.Func, vectorize: bool = False, engine: Optional[Engine] = 
             else:
                 cargs.append(v)
         cfn(*cargs)
+        if table_out:
+            if not out.value:
+                raise _capi.RfError(_capi.RF_ERR_DEVICE, "the query function returned no table: " +
+                                    eng.lib.rf_last_error(eng.h).decode(errors="replace"))
+            return HostArrowTable(out.value)
         return from_c(out)
 
     call.plan = plan
@@ -429,3 +444,18 @@ class _RefTable(ctypes.Structure):
         r = _RefTable(None, t.dim, ctypes.pointer(s), ctypes.pointer(a), None)
         r._keep = (s, a)
         return r
+
+
+class HostArrowTable:
+    """A table result of a query function: the host ArrowTable at `addr` (Reffine's layout,
+    abi.h:56-69), owned by the plan that made it."""
+
+    def __init__(self, addr: int):
+        self.ref = _RefTable.from_address(addr)
+
+    @property
+    def num_rows(self) -> int:
+        return int(self.ref.array.contents.length)
+
+    def to_dict(self) -> Dict:
+        return arrow_to_dict(self.ref.schema.contents, self.ref.array.contents)
