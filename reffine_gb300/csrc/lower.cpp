@@ -614,7 +614,12 @@ private:
                 case MathOp::SQRT: return scalar("sqrt(" + a(0) + ")", n.type);
                 case MathOp::CEIL: return scalar("ceil(" + a(0) + ")", n.type);
                 case MathOp::FLOOR: return scalar("floor(" + a(0) + ")", n.type);
-                case MathOp::POW: return scalar("pow(" + a(0) + ", " + a(1) + ")", n.type);
+                case MathOp::POW:
+                    // single precision through the double pow, rounded once: within CUDA's documented
+                    // double pow error of the host's correctly rounded powf, where powf alone is 2 ulp
+                    if (n.type.btype == FLOAT32)
+                        return scalar("((float)pow((double)(" + a(0) + "), (double)(" + a(1) + ")))", n.type);
+                    return scalar("pow(" + a(0) + ", " + a(1) + ")", n.type);
                 case MathOp::ABS:
                     if (n.type.is_float()) return scalar("fabs(" + a(0) + ")", n.type);
                     return scalar("((" + T + ")llabs((long long)(" + a(0) + ")))", n.type);
