@@ -24,7 +24,9 @@ Parity notes (where this restatement pins the reference's exact behaviour):
 Deviations (reference behaviour is undefined or does not compile): ``abs``/``pow`` are emitted
 as real function calls (the reference prints ``|x|`` and ``^``, cemitter.cpp:129-136), and a
 hash probe of an absent key yields row -1, which ``readdata`` turns into a zero value instead of
-reading out of bounds.
+reading out of bounds (as it does for a row past the column's end).  A union of two vectors
+walks both from their first rows, and a side past its end takes no further part (the reference
+reads past it).
 """
 from __future__ import annotations
 
@@ -77,7 +79,9 @@ static inline int64_t rf_vector_locate(const rf_otable* t, int64_t key) {
     while (ix->vals[h] >= 0) { if (ix->keys[h] == key) return ix->vals[h]; h = (h + 1) & m; }
     return -1; }
 template <class T> static inline T rf_read(const rf_otable* t, int col, int64_t idx) {
-    if (idx < 0) return T(0); return ((const T*)t->cols[col].data)[idx]; }
+    if (idx < 0 || idx >= t->cols[col].len) return T(0); return ((const T*)t->cols[col].data)[idx]; }
+// a merge side past its last row takes no further part in a union's walk
+#define RF_ITER_END INT64_MAX
 static inline void rf_out_init(rf_oout* o, int64_t ncols, const int64_t* esize) {
     o->len = 0; o->cap = 0; o->null_count = 0; o->ncols = ncols; o->bytemap = nullptr;
     for (int64_t i = 0; i < ncols; i++) { o->cols[i] = nullptr; o->esize[i] = esize[i]; } }
@@ -311,6 +315,39 @@ def _tsel(c, a, b):
 
 
 class Union(Joint):
+    """UnionSpace (iter_space.cpp:278-316) over two merged vectors.  Where both sides are alive
+    this is the reference's walk: the iterator is the smaller of the two current keys and the
+    side(s) holding it advance; element reads use each side's current row.  The reference's walk
+    is undefined at the tails (it reads an exhausted side past its end, and Locate of the lower
+    bound on the side that lacks it gives row -1); here both sides start at their first row and
+    a side past its end takes no further part (its key counts as larger than any)."""
+
+    def _plain(self):
+        return isinstance(self.left, VecSpace) and isinstance(self.right, VecSpace)
+
+    def _side_iter(self, g, sp, i):
+        return "(%s ? %s : RF_ITER_END)" % (sp.is_alive(g, i), sp.idx_to_iter(g, i))
+
+    def idx_to_iter(self, g, idx):
+        if not self._plain():
+            return Joint.idx_to_iter(self, g, idx)
+        return "RF_MIN(%s, %s)" % (self._side_iter(g, self.left, idx[0]), self._side_iter(g, self.right, idx[1]))
+
+    def iter_to_idx(self, g, it):
+        if not self._plain():
+            return Joint.iter_to_idx(self, g, it)
+        return ("int64_t(0)", "int64_t(0)")
+
+    def next(self, g, idx):
+        if not self._plain():
+            return Joint.next(self, g, idx)
+        li = self._side_iter(g, self.left, idx[0])
+        ri = self._side_iter(g, self.right, idx[1])
+        lc, rc = g.fresh("lcond"), g.fresh("rcond")
+        g.emit("bool %s = (%s <= %s);" % (lc, li, ri))
+        g.emit("bool %s = (%s <= %s);" % (rc, ri, li))
+        return (_tsel(lc, self.left.next(g, idx[0]), idx[0]), _tsel(rc, self.right.next(g, idx[1]), idx[1]))
+
     def lower_bound(self, g):
         l, r = self.left.lower_bound(g), self.right.lower_bound(g)
         return "RF_MIN(%s, %s)" % (l, r) if (l and r) else (l or r)

@@ -12,6 +12,7 @@
 #include "lower.h"
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -1583,13 +1584,58 @@ private:
         for (auto& d : dcls) pieces.push_back(&d);
         std::string condtext = rowcond + allconds;
         std::string hoisted = hoist_row_loads(condtext, pieces);
-        row << "RF_DEV void rf_row(const RfParams& P, long long r, RfAcc& A)\n{\n";
-        row << body.str() << hoisted;
+        // the hoisted loads ("    const T ldK = rf_ld<T>(COL.data, r);") become parameters of the
+        // row body rf_row_v, so that rf_row (one row) and rf_row4 (4 rows from vector loads) share it
+        std::vector<std::array<std::string, 3>> hl;  // type, name, column pointer
+        {
+            std::istringstream in(hoisted);
+            std::string line;
+            while (std::getline(in, line)) {
+                size_t c = line.find("const "), eq = line.find(" = rf_ld<"), open = line.find(">(", eq);
+                size_t end = line.rfind(", r);");
+                if (c == std::string::npos || eq == std::string::npos || open == std::string::npos || end == std::string::npos) {
+                    hl.clear();
+                    break;
+                }
+                std::string decl = line.substr(c + 6, eq - c - 6);
+                size_t sp = decl.rfind(' ');
+                hl.push_back({decl.substr(0, sp), decl.substr(sp + 1), line.substr(open + 2, end - open - 2)});
+            }
+        }
+        const bool vec4 = !hl.empty() && plan_.kind == PlanKind::SCAN_REDUCE;
+        if (vec4) {
+            row << "RF_DEV void rf_row_v(const RfParams& P, long long r, RfAcc& A";
+            for (auto& h : hl) row << ", const " << h[0] << " " << h[1];
+            row << ")\n{\n" << body.str();
+        } else {
+            row << "RF_DEV void rf_row(const RfParams& P, long long r, RfAcc& A)\n{\n";
+            row << body.str() << hoisted;
+        }
         for (auto& dcl : dcls) row << "    " << dcl << "\n";
         row << "    if (!(" << rowcond << ")) return;\n";
         row << updates;
         if (act.empty()) row << "    (void)A;\n";
         row << "}\n\n";
+        if (vec4) {
+            row << "RF_DEV void rf_row(const RfParams& P, long long r, RfAcc& A)\n{\n" << hoisted;
+            row << "    rf_row_v(P, r, A";
+            for (auto& h : hl) row << ", " << h[1];
+            row << ");\n}\n\n";
+            row << "#define RF_VEC4 1\n";
+            row << "RF_DEV void rf_row4(const RfParams& P, long long r, RfAcc& A)\n{\n";
+            for (auto& h : hl) {
+                // bool columns are read as bytes (any nonzero byte is true, as rf_ld<bool> reads them)
+                std::string lt = h[0] == "bool" ? "int8_t" : h[0];
+                row << "    " << lt << " " << h[1] << "[4];\n    rf_ld4<" << lt << ">(" << h[2] << ", r, " << h[1] << ");\n";
+            }
+            for (int q = 0; q < 4; q++) {
+                row << "    rf_row_v(P, r + " << q << ", A";
+                for (auto& h : hl) row << ", " << (h[0] == "bool" ? "(" + h[1] + "[" + std::to_string(q) + "] != 0)"
+                                                              : h[1] + "[" + std::to_string(q) + "]");
+                row << ");\n";
+            }
+            row << "}\n\n";
+        }
         src << row.str();
     }
 
@@ -2759,6 +2805,291 @@ extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_con
         plan_.source = o.str();
     }
 
+    // Op over the union of two vectors (UnionSpace, iter_space.cpp:278-316, walked as JointSpace,
+    // :217-250): Op([t], In(t, A) | In(t, B), outputs) over two 1-d vectors with sorted iterator
+    // columns.  The walk visits the merged key sequence: at each step t is the smaller of the two
+    // current keys, the side(s) holding t advance, and Element(A, t) / Element(B, t) read each
+    // side's current row (the row holding t, or the lagging side's next row).  Both sides start
+    // at row 0 and a side past its end takes no further part (its reads give 0).
+    // A key v held cA times in A and cB times in B takes max(cA, cB) visits; visit j of v pairs
+    // A row lA(v) + j with B row lB(v) + j while both exist.  Its position in the walk is
+    //     lA(v) + lB(v) - M(lA(v)) + j,
+    // lX(v) the first row of X with key >= v and M(i) the number of paired A rows before row i.
+    // Kernels: rf_u_flags marks each paired A row, an exclusive scan gives M, rf_u_total the
+    // number of visits, and rf_u_emit lets every A row and every unpaired B row write its visit
+    // at its position - no compaction pass.  iter_cond (a side alive with a valid iterator) is
+    // the validity bit of a vectorised output; without vectorize every visit is a row (inputs
+    // whose iterator columns hold nulls are refused at run time then).
+    void lower_union_op(const Op& op, const Expr& left, const Expr& right)
+    {
+        plan_.kind = PlanKind::UNION_MERGE;
+        const int T = plan_.threads;
+        if (op.iters.size() != 1) throw LowerError("union over several iterators");
+        const Expr& it = op.iters[0];
+        if (!(it->type == types::INT64_T || it->type.is_idx())) throw LowerError("union over a non-int64 iterator");
+        int in[2];
+        Expr vec[2];
+        const Expr sides[2] = {resolve(left), resolve(right)};
+        for (int k = 0; k < 2; k++) {
+            if (sides[k]->kind != NodeKind::IN) throw LowerError("a union of iteration spaces other than two vectors");
+            auto i = as<In>(sides[k]);
+            if (i->iter.get() != it.get()) throw LowerError("union over another iterator");
+            vec[k] = resolve(i->vec);
+            auto f = input_index_.find(vec[k].get());
+            if (f == input_index_.end()) throw LowerError("union over a non-input vector");
+            in[k] = f->second;
+            const DataType& vt = fn_->inputs[in[k]]->type;
+            if (vt.dim != 1) throw LowerError("union over a 2-d vector");
+            if (!(vt.dtypes[0] == types::INT64_T || vt.dtypes[0].is_idx())) throw LowerError("union over non-int64 keys");
+            note_col(in[k], 0);
+        }
+        if (in[0] == in[1]) throw LowerError("union of a vector with itself");
+        // no driving table: the walk's domain is both vectors' rows (nA + nB), not one table's
+        plan_.drive_input = -1;
+        {
+            HostExpr lo, a, b, sum;
+            lo.kind = HostExpr::CONST;
+            lo.value = 0;
+            a.kind = b.kind = HostExpr::LEN;
+            a.input = in[0];
+            b.input = in[1];
+            a.col = b.col = 0;
+            sum.kind = HostExpr::ADD;
+            sum.args = {a, b};
+            plan_.row_lo = lo;
+            plan_.row_hi = sum;
+        }
+        plan_.device_range = false;
+        plan_.union_inputs[0] = in[0];
+        plan_.union_inputs[1] = in[1];
+        const std::string A = "P.t[" + std::to_string(plan_.table_slot[in[0]]) + "].col[0]";
+        const std::string B = "P.t[" + std::to_string(plan_.table_slot[in[1]]) + "].col[0]";
+        std::ostringstream o;
+        o << "// generated by the reffine_gb300 lowering pass: " << fn_->name << " (union merge co-iteration)\n";
+        o << "#include \"rf_device.cuh\"\n\n";
+        o << "// first row of sorted int64 column c (n rows) whose key is >= key (> key when upper)\n";
+        o << "RF_DEV long long rf_u_bound(const RfCol& c, long long n, long long key, bool upper)\n{\n";
+        o << "    long long lo = 0, hi = n;\n    const long long* k = (const long long*)c.data;\n";
+        o << "    while (lo < hi) {\n        const long long m = (lo + hi) >> 1;\n        const long long x = __ldg(k + m);\n";
+        o << "        if (x < key || (upper && x == key)) lo = m + 1; else hi = m;\n    }\n    return lo;\n}\n\n";
+        o << "extern \"C\" __global__ void __launch_bounds__(256) rf_u_flags(const __grid_constant__ RfParams P)\n{\n";
+        o << "    long long* M = (long long*)P.aux4;\n    const long long nA = " << A << ".len, nB = " << B << ".len;\n";
+        o << "    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nA; i += (long long)gridDim.x * blockDim.x) {\n";
+        o << "        const long long v = rf_ld<int64_t>(" << A << ".data, i);\n";
+        o << "        const long long a = i - rf_u_bound(" << A << ", nA, v, false);\n";
+        o << "        const long long lB = rf_u_bound(" << B << ", nB, v, false), cB = rf_u_bound(" << B << ", nB, v, true) - lB;\n";
+        o << "        M[i] = a < cB ? 1 : 0;\n    }\n";
+        o << "    if (blockIdx.x == 0 && threadIdx.x == 0) M[nA] = 0;\n}\n\n";
+        o << "extern \"C\" __global__ void rf_u_total(const __grid_constant__ RfParams P)\n{\n";
+        o << "    if (threadIdx.x != 0 || blockIdx.x != 0) return;\n";
+        o << "    const long long nA = " << A << ".len, nB = " << B << ".len;\n";
+        o << "    ((long long*)P.aux3)[0] = nA + nB - ((const long long*)P.aux4)[nA];\n}\n\n";
+        // the visit's outputs
+        Emitter E(*this);
+        bind_inputs(E);
+        E.in_bounds_rows = false;
+        E.vec_iter_idx[{vec[0].get(), it.get()}] = "li";
+        E.vec_iter_idx[{vec[1].get(), it.get()}] = "ri";
+        E.bind(op.iters[0], E.scalar("it", it->type));
+        std::ostringstream w;
+        size_t c = 0;
+        w << "    ((" << ctype(it->type) << "*)((void* const*)P.aux0)[" << c++ << "])[o] = it;\n";
+        for (auto& x : op.outputs) {
+            w << "    ((" << ctype(x->type) << "*)((void* const*)P.aux0)[" << c << "])[o] = (" << ctype(x->type) << ")("
+              << E.ev(x).c << ");\n";
+            c++;
+        }
+        o << "RF_DEV void rf_u_write(const RfParams& P, long long li, long long ri, long long v, long long o)\n{\n";
+        o << "    const " << ctype(it->type) << " it = (" << ctype(it->type) << ")v;\n";
+        for (auto& dcl : E.decls) o << "    " << dcl << "\n";
+        o << w.str() << "}\n\n";
+        o << "extern \"C\" __global__ void __launch_bounds__(" << T << ") rf_u_emit(const __grid_constant__ RfParams P)\n{\n";
+        o << "    const long long* M = (const long long*)P.aux4;\n    const long long nA = " << A << ".len, nB = " << B
+          << ".len;\n    const long long V = ((const long long*)P.aux3)[0];\n    long long nulls = 0;\n";
+        o << "    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nA + nB; r += (long long)gridDim.x * blockDim.x) {\n";
+        o << "        long long v, li, ri, pos;\n";
+        o << "        if (r < nA) {\n            li = r;\n            v = rf_ld<int64_t>(" << A << ".data, li);\n";
+        o << "            const long long lA = rf_u_bound(" << A << ", nA, v, false), a = li - lA;\n";
+        o << "            const long long lB = rf_u_bound(" << B << ", nB, v, false), cB = rf_u_bound(" << B << ", nB, v, true) - lB;\n";
+        o << "            ri = a < cB ? lB + a : lB + cB;\n            pos = lA + lB - M[lA] + a;\n";
+        o << "        } else {\n            ri = r - nA;\n            v = rf_ld<int64_t>(" << B << ".data, ri);\n";
+        o << "            const long long lB = rf_u_bound(" << B << ", nB, v, false), b = ri - lB;\n";
+        o << "            const long long lA = rf_u_bound(" << A << ", nA, v, false), cA = rf_u_bound(" << A << ", nA, v, true) - lA;\n";
+        o << "            if (b < cA) continue;  // paired with A row lA + b, which writes the visit\n";
+        o << "            li = lA + cA;\n            pos = lA + lB - M[lA] + b;\n        }\n";
+        // keys out of order (the walk needs sorted iterator columns) can only move a visit, never
+        // past the output: positions are checked against the visit count
+        o << "        if (pos < 0 || pos >= V) { rf_set_err(P, RF_DEVERR_RANGE); continue; }\n";
+        o << "        rf_u_write(P, li, ri, v, pos);\n";
+        if (vectorize_) {
+            o << "        const bool ok = (li < nA && rf_valid(" << A << ".valid, li)) || (ri < nB && rf_valid(" << B
+              << ".valid, ri));\n";
+            o << "        if (ok)\n            for (int col = 0; col < " << plan_.out_cols.size()
+              << "; col++) atomicOr(((unsigned**)P.aux1)[col] + (pos >> 5), 1u << (pos & 31));\n";
+            o << "        else\n            nulls++;\n";
+        }
+        o << "    }\n";
+        o << "    if (nulls) atomicAdd((unsigned long long*)P.aux3 + 1, (unsigned long long)nulls);\n}\n";
+        plan_.kernels.clear();
+        plan_.kernels.push_back({"rf_u_flags", 256, 0, KernelSpec::SEGCOUNT});
+        plan_.kernels.push_back({"", 0, 0, KernelSpec::SEGSCAN});
+        plan_.kernels.push_back({"rf_u_total", 32, 0, KernelSpec::RANGE});
+        plan_.kernels.push_back({"rf_u_emit", T, 0, KernelSpec::SCATTER});
+        plan_.source = o.str();
+    }
+
+    // Op over several iterators (NestedSpace, iter_space.cpp:366-452): the loop nest visits the
+    // outer iterator's range and, for each of its values, the inner ones in order.  Lowered here
+    // for rectangular nests: every iterator ranges over bounds of constants and scalar inputs
+    // (no vector, no bound that names another iterator).  The nest's visits are numbered in loop
+    // order and each number is decomposed into the iterators' values.  As in the reference's
+    // loop, an inner level that runs past its upper bound is visited once more (iter_cond false,
+    // a null row of the vectorised output) before the next outer value resets it: a level j > 0
+    // with n_j values takes S_j = n_j * S_{j+1} + 1 visits (S_k = 1 past the innermost), the
+    // outermost n_0 * S_1.  The non-vectorised output keeps the valid visits, in order.
+    void lower_nested_op(const Op& op)
+    {
+        plan_.kind = PlanKind::MATERIALIZE;
+        const int T = plan_.threads;
+        const size_t K = op.iters.size();
+        std::set<const ExprNode*> vars;
+        for (auto& s : fn_->inputs)
+            if (s->type.is_val()) vars.insert(s.get());
+        std::vector<Space> sps(K);
+        for (size_t j = 0; j < K; j++) {
+            Space& sp = sps[j];
+            sp.iter = op.iters[j];
+            if (!(sp.iter->type.is_int() || sp.iter->type.is_idx())) throw LowerError("nested Op over a non-integer iterator");
+            space_of(op.pred, sp.iter, vars, sp);
+            if (sp.has_vec) throw LowerError("nested Op over a vector is not lowered");
+            if (sp.lbs.empty() || sp.ubs.empty()) throw LowerError("unbounded iteration space in a nested Op");
+            for (auto* bs : {&sp.lbs, &sp.ubs})
+                for (auto& b : *bs)
+                    for (auto& it : op.iters)
+                        if (mentions(b, it.get(), fn_->tbl)) throw LowerError("nested Op bound over another iterator");
+            for (auto& f : sp.filters)
+                for (auto& it : op.iters)
+                    if (it.get() != sp.iter.get() && mentions(f, it.get(), fn_->tbl))
+                        throw LowerError("nested Op filter over another iterator");
+        }
+        // host-side visit count: n_j = max(U_j - L_j + 1, 0)
+        auto n_host = [&](const Space& sp) {
+            HostExpr one, zero, up, d, n;
+            one.kind = HostExpr::CONST;
+            one.value = 1;
+            zero.kind = HostExpr::CONST;
+            zero.value = 0;
+            up.kind = HostExpr::ADD;
+            up.args = {minmax_host(sp.ubs, false), one};
+            d.kind = HostExpr::SUB;
+            d.args = {up, minmax_host(sp.lbs, true)};
+            n.kind = HostExpr::MAX;
+            n.args = {d, zero};
+            return n;
+        };
+        HostExpr S;
+        S.kind = HostExpr::CONST;
+        S.value = 1;
+        for (size_t j = K; j-- > 0;) {
+            HostExpr m;
+            m.kind = HostExpr::MUL;
+            m.args = {n_host(sps[j]), S};
+            if (j > 0) {
+                HostExpr one, a;
+                one.kind = HostExpr::CONST;
+                one.value = 1;
+                a.kind = HostExpr::ADD;
+                a.args = {m, one};
+                S = a;
+            } else {
+                S = m;
+            }
+        }
+        HostExpr lo;
+        lo.kind = HostExpr::CONST;
+        lo.value = 0;
+        plan_.row_lo = lo;
+        plan_.row_hi = S;
+        plan_.device_range = false;
+        std::ostringstream src;
+        src << "// generated by the reffine_gb300 lowering pass: " << fn_->name << " (nested Op)\n";
+        src << "#include \"rf_device.cuh\"\n\n";
+        // decomposition of visit r into the iterators it0..it{K-1} and its validity
+        auto bind_nest = [&](Emitter& E, std::ostringstream& b) -> std::string {
+            bind_inputs(E);
+            for (size_t j = 0; j < K; j++) {
+                std::string Tj = ctype(sps[j].iter->type), J = std::to_string(j);
+                b << "    const long long L" << J << " = (long long)(" << bound_expr(E, sps[j].lbs, "", true, sps[j].iter->type)
+                  << ");\n";
+                b << "    long long n" << J << " = (long long)(" << bound_expr(E, sps[j].ubs, "", false, sps[j].iter->type)
+                  << ") - L" << J << " + 1;\n    if (n" << J << " < 0) n" << J << " = 0;\n";
+            }
+            // S_j: visits of level j's block (S_K = 1)
+            b << "    long long S" << K << " = 1;\n";
+            for (size_t j = K; j-- > 1;)
+                b << "    const long long S" << j << " = n" << j << " * S" << j + 1 << " + 1;\n";
+            b << "    bool ok = true;\n    long long p = r;\n";
+            for (size_t j = 0; j < K; j++) {
+                std::string J = std::to_string(j), J1 = std::to_string(j + 1);
+                b << "    long long i" << J << ";\n";
+                if (j == 0) {
+                    b << "    i0 = L0 + p / S1;\n    p = p % S1;\n";
+                } else {
+                    b << "    if (!ok) { i" << J << " = L" << J << "; }\n";
+                    b << "    else if (p == n" << J << " * S" << J1 << ") { i" << J << " = L" << J << " + n" << J
+                      << "; ok = false; }\n";
+                    b << "    else { i" << J << " = L" << J << " + p / S" << J1 << "; p = p % S" << J1 << "; }\n";
+                }
+                b << "    const " << ctype(sps[j].iter->type) << " it" << J << " = (" << ctype(sps[j].iter->type) << ")i"
+                  << J << ";\n";
+                E.bind(op.iters[j], E.scalar("it" + J, sps[j].iter->type));
+            }
+            b << "    (void)p;\n";
+            std::string cond = "ok";
+            for (auto& sp : sps)
+                for (auto& f : sp.filters) cond += " && (" + E.ev(f).c + ")";
+            return cond;
+        };
+        {
+            Emitter E(*this);
+            std::ostringstream b;
+            std::string cond = bind_nest(E, b);
+            src << "RF_DEV bool rf_cond(const RfParams& P, long long r)\n{\n" << b.str();
+            for (auto& dcl : E.decls) src << "    " << dcl << "\n";
+            src << "    return " << cond << ";\n}\n\n";
+        }
+        {
+            Emitter E(*this);
+            std::ostringstream b;
+            bind_nest(E, b);
+            std::ostringstream w;
+            size_t c = 0;
+            for (auto& i : op.iters) {
+                w << "    ((" << ctype(i->type) << "*)((void* const*)P.aux0)[" << c << "])[o] = (" << ctype(i->type)
+                  << ")(" << E.ev(i).c << ");\n";
+                c++;
+            }
+            for (auto& x : op.outputs) {
+                w << "    ((" << ctype(x->type) << "*)((void* const*)P.aux0)[" << c << "])[o] = (" << ctype(x->type)
+                  << ")(" << E.ev(x).c << ");\n";
+                c++;
+            }
+            src << "RF_DEV void rf_emit(const RfParams& P, long long r, long long o)\n{\n" << b.str();
+            for (auto& dcl : E.decls) src << "    " << dcl << "\n";
+            src << w.str() << "}\n\n";
+        }
+        src << "#define RF_MATERIALIZE 1\n#include \"rf_templates.cuh\"\n";
+        src << "RF_MATERIALIZE_KERNELS(" << T << ", " << plan_.out_cols.size() << ")\n";
+        if (vectorize_) {
+            plan_.kernels.push_back({"rf_write_all", T, 0, KernelSpec::FINAL});
+        } else {
+            plan_.kernels.push_back({"rf_count", T, 0, KernelSpec::COUNT});
+            plan_.kernels.push_back({"rf_scan", 1024, 0, KernelSpec::SCAN});
+            plan_.kernels.push_back({"rf_scatter", T, 0, KernelSpec::SCATTER});
+        }
+        plan_.source = src.str();
+    }
+
     void lower_op(const Expr& opx)
     {
         const Op& op = *as<Op>(opx);
@@ -2770,6 +3101,17 @@ extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_con
             plan_.out_cols.push_back(o->type);
         }
         if ((int)plan_.out_cols.size() > RF_MAX_COLS_) throw LowerError("too many output columns");
+        if (op.iters.size() > 1) {
+            lower_nested_op(op);
+            return;
+        }
+        {
+            Expr pred = resolve(op.pred);
+            if (is_nary(pred, MathOp::OR)) {
+                lower_union_op(op, as<NaryExpr>(pred)->args[0], as<NaryExpr>(pred)->args[1]);
+                return;
+            }
+        }
         Drive d;
         d.sp = op_space(op);
         drive_rows(d);

@@ -26,6 +26,7 @@ enum class PlanKind {
     SEG_REDUCE = 4,    // Op over a run-end encoded 2-d vector with a nested Reduce per run
     HASH_GROUP = 5,    // the same query over an unsorted flat key column: hash group-by
     MERGE_JOIN = 6,    // Op over an intersection of vectors (merge co-iteration)
+    UNION_MERGE = 7,   // Op over a union of two vectors (outer merge co-iteration)
 };
 
 struct LowerError : std::runtime_error {
@@ -84,6 +85,7 @@ struct Plan {
     size_t acc_bytes = 0;               // bytes of one unit's partial (scan-reduce, segmented reduce)
     int seg_chunk = 256;                // segmented reduce: rows per chunk
     int ixf_input = -1;                 // input whose index a run replaces by a filtered one (-1: none)
+    int union_inputs[2] = {-1, -1};     // union merge: the two merged vectors (Func inputs)
     int hg_hot = 0;                     // hash group-by: hottest keys folded per warp (index 2x)
     int hg_warm = 0;                    // hash group-by: further hot keys in shared memory (index 2x)
     int groups = 0, aggs = 0;           // grouped plans

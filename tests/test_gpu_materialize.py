@@ -153,3 +153,100 @@ def test_merge_join_sorted_with_gaps_and_duplicates(eng):
     fn.tbl[os_] = op
     out = plan_run_table(eng, eng.compile(fn), ta, tb)
     assert_table_same(out, loopgen.Query(fn)(ta, tb))
+
+
+def _nest3(ub_a, ub_b, ub_c):
+    """A three-level nest with scalar bounds: Op([a, b, c], 0 <= a < A & 1 <= b <= B & -2 <= c < C,
+    [a * 100 + b * 10 + c, b - c])."""
+    from reffine_gb300.ir import _mul, _sub
+    a, b, c = _sym("a", _i64_t), _sym("b", _i64_t), _sym("c", _i64_t)
+    A, B, C = _sym("A", _i64_t), _sym("B", _i64_t), _sym("C", _i64_t)
+    pred = (_gte(a, _i64(0)) & _lt(a, A) & _gte(b, _i64(1)) & _lte(b, B) & _gte(c, _i64(-2)) & _lt(c, C))
+    op = _op([a, b, c], pred, [_add(_add(_mul(a, _i64(100)), _mul(b, _i64(10))), c), _sub(b, c)])
+    op_sym = _sym("op", op)
+    fn = _func("nest3", op_sym, [A, B, C])
+    fn.tbl[op_sym] = op
+    return fn
+
+
+@pytest.mark.parametrize("vectorize", [False, True])
+def test_nested_op_identities(eng, vectorize):
+    # NestedOpTest (test_nested.cpp:29-53): every valid row of the 10 x 10 nest in order, with
+    # a = idx / 10, b = idx % 10 and a + b; vectorised, each inner loop's end is a null row
+    fn = rq.nested_op(10, 10)
+    plan = eng.compile(fn, vectorize)
+    out = plan_run_table(eng, plan)
+    ref = loopgen.Query(fn, vectorize)()
+    assert_table_same(out, ref)
+    valid = np.ones(out["len"], bool) if out["valid"][0] is None else out["valid"][0]
+    idx = 0
+    for i in range(out["len"]):
+        if valid[i]:
+            assert (out["cols"][0][i], out["cols"][1][i], out["cols"][2][i]) == (idx // 10, idx % 10, idx // 10 + idx % 10)
+            idx += 1
+    assert idx == 100
+    assert out["len"] == (110 if vectorize else 100)
+
+
+@pytest.mark.parametrize("vectorize", [False, True])
+@pytest.mark.parametrize("bounds", [(3, 4, 2), (1, 1, -2), (4, 0, 3), (0, 5, 5), (7, 30, 40)])
+def test_nested_op_three_levels(eng, vectorize, bounds):
+    # scalar bounds, empty levels included: the same rows, nulls and values as the oracle's loop
+    fn = _nest3(*bounds)
+    plan = eng.compile(fn, vectorize)
+    out = plan_run_table(eng, plan, *bounds)
+    ref = loopgen.Query(fn, vectorize)(*bounds)
+    assert_table_same(out, ref)
+    if vectorize and ref["valid"] is not None:
+        np.testing.assert_array_equal(out["valid"][0], ref["valid"])
+
+
+def union_op(ta, tb):
+    """An outer merge as the reference's micro benchmark writes it (micro.h:83-102, ojoin_op): Op
+    over In(t, left) | In(t, right) with lval - rval, plus each side's value."""
+    from reffine_gb300.ir import _sub
+    tt = _sym("t", _i64_t)
+    left, right = _sym("left", ta.get_data_type()), _sym("right", tb.get_data_type())
+    lval, rval = _get(left[tt], 0), _get(right[tt], 0)
+    op = _op([tt], _in(tt, left) | _in(tt, right), [_sub(lval, rval), lval, rval])
+    os_ = _sym("op", op)
+    fn = _func("ojoin", os_, [left, right])
+    fn.tbl[os_] = op
+    return fn
+
+
+def _sorted_table(rng, n, hi):
+    k = np.sort(rng.integers(0, hi, n)).astype(np.int64)
+    return Table.from_arrays(1, {"k": k, "v": rng.integers(-1000, 1000, n).astype(np.int64)})
+
+
+@pytest.mark.parametrize("vectorize", [False, True])
+@pytest.mark.parametrize("sizes", [(1000, 700, 500), (0, 50, 100), (50, 0, 100), (1, 1, 3), (200_003, 150_001, 120_000),
+                                   (1_000_000, 1_000_000, 3_000_000)])
+def test_union_merge_matches_oracle(eng, vectorize, sizes):
+    # duplicates on both sides, keys on one side only, empty sides, sides that end first
+    na, nb, hi = sizes
+    rng = np.random.default_rng(na + nb)
+    ta, tb = _sorted_table(rng, na, hi), _sorted_table(rng, nb, hi)
+    fn = union_op(ta, tb)
+    plan = eng.compile(fn, vectorize)
+    assert plan.kind == 7
+    out = plan_run_table(eng, plan, ta, tb)
+    ref = loopgen.Query(fn, vectorize)(ta, tb)
+    assert_table_same(out, ref)
+    # the walk visits every key of either side: max(count in left, count in right) times each
+    ka, kb = ta.columns[0].data, tb.columns[0].data
+    keys = np.union1d(ka, kb)
+    expect = sum(max(int((ka == k).sum()), int((kb == k).sum())) for k in keys) if len(keys) < 5000 else None
+    if expect is not None:
+        assert out["len"] == expect
+
+
+def test_union_merge_of_one_table_with_itself(eng):
+    # main.cpp:386-400 (shift_op): the same table on both sides pairs every row with itself
+    rng = np.random.default_rng(9)
+    t = _sorted_table(rng, 10_000, 4_000)
+    u = Table.from_arrays(1, {"k": t.columns[0].data.copy(), "v": t.columns[1].data.copy()})
+    out = plan_run_table(eng, eng.compile(union_op(t, u)), t, u)
+    assert out["len"] == 10_000
+    np.testing.assert_array_equal(out["cols"][1], np.zeros(10_000, dtype=np.int64))
