@@ -23,8 +23,10 @@ GB/s = algorithmic bytes (each referenced column read once) / time.
 
 --impl reference times the oracle port alone (the reference's CPU path; it is single-threaded);
 it counts bytes from the columns each workload declares and loads nothing of the GPU backend.
-Multi-GPU (torchrun): each rank scans its own partition (weak scaling), no collective on the
-data path; rank 0 prints the max-over-ranks time.
+Multi-GPU (torchrun): each rank scans its own partition (weak scaling; a join's build side is
+the same on every rank), no collective on the data path; rank 0 prints the max-over-ranks time.
+After the timed steps each rank's partial state is gathered to rank 0 and folded in rank order
+into one answer ("sharded": reffine_gb300.shard).
 """
 from __future__ import annotations
 
@@ -78,6 +80,14 @@ class Dist:
         t = torch.tensor([x], dtype=torch.float64)
         self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
         return float(t.item())
+
+    def gather(self, obj):
+        """Every rank's object on rank 0, in rank order (None elsewhere)."""
+        if self.world == 1:
+            return [obj]
+        out = [None] * self.world if self.td.get_rank() == 0 else None
+        self.td.gather_object(obj, out, dst=0)
+        return out
 
     def sum(self, x: float) -> float:
         if self.world == 1:
@@ -179,7 +189,8 @@ def build_workload(config: int, rank: int, world: int, rows: int = 0) -> Workloa
         return Workload(name, [t], W.hashgroup_query(t.get_data_type()), n, build_cfg(2, n), [[0, 1]])
     if config == 3:
         nb, npr = 10_000_000, rows or 200_000_000
-        b, p = W.join_tables(nb, npr, seed=3 + seed_off)
+        # every rank holds the same build side; probe rows are the rank's own partition
+        b, p = W.join_tables(nb, npr, seed=3, probe_seed=None if world == 1 else 3 + seed_off)
         return Workload(name, [b, p], W.join_query(b.get_data_type(), p.get_data_type()), npr, build_cfg(3, npr),
                         [[0, 1], [1, 2, 3]])
     raise SystemExit("config %d is not benchmarked by this script" % config)
@@ -492,10 +503,40 @@ def measure_config(eng, wl: Workload, config: int, args, rank: int, world: int, 
         res["cpu_baseline"] = None
         res["parity"] = None
     res["result_sample"] = ("%d output rows" % out_rows[0]) if table_out else str(got)[:200]
+    if world > 1:
+        res["sharded"] = shard_fold(eng, wl, dts, got, dist, rank, world)
     for d in dts:
         d.free()
     plan.free()
     return res
+
+
+def shard_fold(eng, wl: Workload, dts, got, dist, rank: int, world: int) -> dict:
+    """One answer over all ranks' partitions (after the timed steps): each rank's partial Reduce
+    state (or partial grouped table) from its GPU, gathered to rank 0 and folded in rank order
+    (reffine_gb300.shard)."""
+    from reffine_gb300 import shard
+    t0 = time.perf_counter()
+    if isinstance(got, dict):
+        part = {"cols": got["cols"], "len": got["len"]}
+    else:
+        state_fn, _ = shard.split_reduce(wl.fn)
+        sp = eng.compile(state_fn)
+        part = sp.run(*dts)
+        sp.free()
+    parts = dist.gather(part)
+    if rank != 0:
+        return None
+    if isinstance(got, dict):
+        folded = shard.fold_tables(parts, ["sum"] * (len(part["cols"]) - 1))
+        sample = "%d groups" % folded["len"]
+    else:
+        _, finish = shard.split_reduce(wl.fn)
+        folded = finish(shard.fold_states(parts, shard.leaf_ops(wl.fn)))
+        sample = str(folded)[:200]
+    return {"ranks": world, "rows_total": wl.rows * world, "fold_ms": (time.perf_counter() - t0) * 1e3,
+            "partition": "each rank its own seeded row range; partial states folded on rank 0 in rank order",
+            "result_sample": sample}
 
 
 def bench_serving(eng, n_queries: int, max_rows: int, rates=(0.5, 0.8, 1.0, 1.5), table_lanes: int = 0,

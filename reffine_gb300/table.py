@@ -132,6 +132,20 @@ class Table:
             out.append(Column(nm, t, arr, v, re))
         return Table(name, dim, out)
 
+    def rows(self, lo: int, hi: int) -> "Table":
+        """Rows [lo, hi) as a table of the same type (flat columns share the values; validity
+        bitmaps are re-packed from bit lo).  A partition of a table for one rank of a sharded
+        query; run-end columns cannot be cut by rows this way."""
+        cols = []
+        for c in self.columns:
+            if c.run_ends is not None:
+                raise ValueError("a row range of a run-end column (%s) is not taken" % c.name)
+            v = None
+            if c.valid is not None:
+                v = pack_validity(unpack_validity(c.valid, len(c.data))[lo:hi])
+            cols.append(Column(c.name, c.dtype, c.data[lo:hi], v))
+        return Table(self.name, self.dim, cols)
+
     def get_data_type(self) -> ir.DataType:
         """ArrowTable2::get_data_type (table.h:62-80)."""
         return ir.DataType("vector", [c.ir_type for c in self.columns], self.dim,

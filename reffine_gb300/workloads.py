@@ -175,10 +175,13 @@ def hashgroup_query(tbl_type: ir.DataType) -> ir.Func:
 Q3_ATTR, Q3_DAY_LO, Q3_DAY_HI = 5, 0, 365
 
 
-def join_tables(n_build: int = 10_000_000, n_probe: int = 200_000_000, seed: int = 3) -> Tuple[Table, Table]:
+def join_tables(n_build: int = 10_000_000, n_probe: int = 200_000_000, seed: int = 3,
+                probe_seed=None) -> Tuple[Table, Table]:
     """Build: unique int64 keys (a seeded sample of a 2^40 space) + attr i32 in [0,25).
     Probe: fk = a uniform build key with p=0.9, else a key from a disjoint range (a miss);
-    amount f64 in [1,10000); day i32 in [0,2557)."""
+    amount f64 in [1,10000); day i32 in [0,2557).  With `probe_seed`, the probe rows come from
+    their own generator (the build side stays that of `seed`): one rank's share of a probe
+    table partitioned over ranks that all hold the same build side."""
     rng = np.random.default_rng(seed)
     # distinct keys: a random odd multiplier permutes the 2^40 space; take n consecutive images
     mult = (int(rng.integers(1, 1 << 39)) << 1) | 1
@@ -186,6 +189,8 @@ def join_tables(n_build: int = 10_000_000, n_probe: int = 200_000_000, seed: int
     keys = ((base * np.uint64(mult)) & np.uint64((1 << 40) - 1)).astype(np.int64)
     attr = rng.integers(0, 25, n_build, dtype=np.int32)
     build = Table.from_arrays(1, {"key": keys, "attr": attr}, name="build")
+    if probe_seed is not None:
+        rng = np.random.default_rng(probe_seed)
     hit = rng.random(n_probe) < 0.9
     fk = keys[rng.integers(0, n_build, n_probe)]
     miss = (np.int64(1) << 41) + rng.integers(0, 1 << 40, n_probe, dtype=np.int64)
