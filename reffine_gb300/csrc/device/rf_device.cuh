@@ -102,6 +102,44 @@ RF_DEV T rf_ld(const void* p, long long i)
     return RfLd<T>::ld(p, i);
 }
 
+// rows r..r+3 of a column (r a multiple of 4, the column 16-byte aligned) in one or two 16-byte
+// streaming loads (4- and 8-byte types; 1- and 2-byte types take one 4- or 8-byte load)
+template <class T>
+RF_DEV void rf_ld4(const void* p, long long r, T* v)
+{
+    const T* b = (const T*)p + r;
+    if constexpr (sizeof(T) == 8) {
+        union {
+            uint4 u[2];
+            T t[4];
+        } x;
+        x.u[0] = __ldcs((const uint4*)b);
+        x.u[1] = __ldcs((const uint4*)(b + 2));
+        v[0] = x.t[0], v[1] = x.t[1], v[2] = x.t[2], v[3] = x.t[3];
+    } else if constexpr (sizeof(T) == 4) {
+        union {
+            uint4 u;
+            T t[4];
+        } x;
+        x.u = __ldcs((const uint4*)b);
+        v[0] = x.t[0], v[1] = x.t[1], v[2] = x.t[2], v[3] = x.t[3];
+    } else if constexpr (sizeof(T) == 2) {
+        union {
+            uint2 u;
+            T t[4];
+        } x;
+        x.u = __ldcs((const uint2*)b);
+        v[0] = x.t[0], v[1] = x.t[1], v[2] = x.t[2], v[3] = x.t[3];
+    } else {
+        union {
+            unsigned int u;
+            T t[4];
+        } x;
+        x.u = __ldcs((const unsigned int*)b);
+        v[0] = x.t[0], v[1] = x.t[1], v[2] = x.t[2], v[3] = x.t[3];
+    }
+}
+
 // guarded read of column `c` at row/run `i` (a located or computed position: cached path)
 template <class T>
 RF_DEV T rf_rd(const RfCol& c, long long i)

@@ -73,6 +73,9 @@ typedef struct RfParams {
 
 #define RF_EMPTY_KEY ((long long)0x8000000000000000ULL)
 
+// RfParams.flags
+#define RF_FLAG_VEC4 1  // every column the driving loop reads is 16-byte aligned: 4-row vector loads
+
 // device error codes written to *err
 #define RF_DEVERR_PROBE 1      // a hash probe/insert visited every slot
 #define RF_DEVERR_WAIT 2       // a bounded wait ran out

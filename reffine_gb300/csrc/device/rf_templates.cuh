@@ -38,6 +38,20 @@ RF_DEV void rf_scan_reduce_rows(const RfParams& P, int unit, int nunits, RfAcc& 
         long long r0 = P.row_lo + tile * tr, r1 = r0 + tr;
         if (r1 > hi) r1 = hi;
         if (r0 < lo) r0 = lo;
+#ifdef RF_VEC4
+        if ((P.flags & RF_FLAG_VEC4) && r0 >= 0) {
+            // a thread takes 4 consecutive rows per step (one 16-byte load per column), in row
+            // order; the rows before the first multiple of 4 and after the last go one by one
+            long long a = (r0 + 3) & ~3LL;
+            if (a > r1) a = r1;
+            const long long b = a + ((r1 - a) & ~3LL);
+            for (long long r = r0 + threadIdx.x; r < a; r += T) rf_row(P, r, acc);
+#pragma unroll 2
+            for (long long r = a + 4 * (long long)threadIdx.x; r < b; r += 4LL * T) rf_row4(P, r, acc);
+            for (long long r = b + threadIdx.x; r < r1; r += T) rf_row(P, r, acc);
+            continue;
+        }
+#endif
 #pragma unroll 4
         for (long long r = r0 + threadIdx.x; r < r1; r += T) rf_row(P, r, acc);
     }

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <list>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -103,6 +104,13 @@ struct rf_ctx {
     std::mutex stage_mu;
     unsigned char* stage = nullptr;
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    // filtered join indexes kept by plans between runs (filtered_index): held under ixf_mu from
+    // the lookup until the run's kernels are enqueued and its event recorded; at most
+    // ixf_budget bytes in all, the plan used longest ago giving its index up first
+    std::mutex ixf_mu;
+    std::list<rf_plan*> ixf_lru;      // plans holding an index, least recently used first
+    size_t ixf_bytes = 0;
+    size_t ixf_budget = 0;
 };
 
 struct DevCol {
@@ -187,6 +195,12 @@ struct rf_plan {
     // filtered index of a probed table (plans with a pushed-down filter): its entry count
     unsigned long long ixf_for = 0;   // generation of the table whose kept-entry count is ixf_count
     long long ixf_count = 0;
+    // ... and the index itself, kept for the next run on the same table (0: none kept)
+    void* ixf_buf = nullptr;
+    size_t ixf_buf_bytes = 0;
+    unsigned long long ixf_buf_for = 0;
+    RfIndex ixf_ix{};
+    cudaEvent_t ixf_ev = nullptr;     // recorded after the last run that read ixf_buf
     // segmented reduce
     long long* seg_woff = nullptr;
     long long* seg_tmp = nullptr;

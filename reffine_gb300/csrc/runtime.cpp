@@ -365,6 +365,12 @@ extern "C" int rf_gpu_init(int device, rf_ctx** out)
     // Grace hosts: the GPU walks the host page tables, so copies from pageable memory run at
     // link speed without a pinned bounce buffer
     cudaDeviceGetAttribute(&ctx->pageable_direct, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+    // filtered join indexes kept between runs: 2 GiB in all unless RF_IXF_CACHE_MB says otherwise
+    // (0 rebuilds every run)
+    {
+        const char* mb = getenv("RF_IXF_CACHE_MB");
+        ctx->ixf_budget = (size_t)(mb ? atoll(mb) : 2048) << 20;
+    }
     CUDA_TRY(nullptr, cudaMalloc((void**)&ctx->dev_err, sizeof(int)));
     CUDA_TRY(nullptr, cudaMemset(ctx->dev_err, 0, sizeof(int)));
     // rf_plan_run_noalloc's fixed array: with lazy module loading the array's device memory is
@@ -1116,10 +1122,19 @@ extern "C" int rf_plan_check(const char* text, int vectorize, char* buf, size_t 
     return RF_OK;
 }
 
+namespace rfrt {
+void release_filtered_index(rf_plan* p, cudaStream_t s);
+}
+
 extern "C" int rf_plan_free(rf_plan* p)
 {
     if (!p) return RF_OK;
     cudaSetDevice(p->ctx->device);
+    {
+        std::lock_guard<std::mutex> g(p->ctx->ixf_mu);
+        rfrt::release_filtered_index(p, p->ctx->stream);
+        if (p->ixf_ev) cudaEventDestroy(p->ixf_ev);
+    }
     cudaStreamSynchronize(p->ctx->stream);
     if (p->buf) cudaFreeAsync(p->buf, p->ctx->stream);
     cudaFree(p->d_tiles);
@@ -1261,9 +1276,15 @@ int fill_params(rf_plan* p, const rf_arg* args, int n_args, RfParams& P, long lo
     if (pl.drive_input >= 0) {
         // never read past the driving table's columns (the reference would read out of bounds)
         rf_table* t = args[pl.drive_input].table;
-        for (int c : pl.cols_read[pl.drive_input])
+        bool aligned = true;
+        for (int c : pl.cols_read[pl.drive_input]) {
             if (t->cols[c].nvals < hi) hi = t->cols[c].nvals;
+            aligned = aligned && ((uintptr_t)t->cols[c].data & 15) == 0;
+        }
         if (lo < 0) lo = 0;
+        // a scan's 4-row vector loads need every column it reads 16-byte aligned (a table loaded
+        // from an IPC file may hold 8-byte aligned buffers; those take the one-row path)
+        if (aligned) P.flags |= RF_FLAG_VEC4;
     }
     if (hi < lo) hi = lo;
     P.row_lo = lo;
@@ -1287,6 +1308,10 @@ bool index_role(int role)
 // pool for this run (*buf; the caller releases it after the probing kernel), and points `out`
 // at it.  The number of entries kept is counted once per table (a synchronising read) and
 // remembered; the entries come from T's rows when no key repeats, else from its index.
+void release_filtered_index(rf_plan* p, cudaStream_t s);
+
+// (the caller holds ctx->ixf_mu from here until the kernels that read the index are enqueued
+// and, when the plan keeps the index, p->ixf_ev is recorded after them)
 int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, RfIndex* out, void** buf)
 {
     rf_ctx* ctx = p->ctx;
@@ -1325,6 +1350,14 @@ int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, R
         p->ixf_count = (long long)n;
         p->ixf_for = T->gen;
     }
+    // the index kept from this plan's last run on the same table (the table's generation
+    // changes with every upload or index build, so a kept index is never stale)
+    if (p->ixf_buf && p->ixf_buf_for == T->gen) {
+        *out = p->ixf_ix;
+        ctx->ixf_lru.remove(p);
+        ctx->ixf_lru.push_back(p);
+        return RF_OK;
+    }
     unsigned long long cap = 64;
     while (cap < 2 * (unsigned long long)p->ixf_count) cap *= 2;
     if (pool_alloc(buf, cap * 16 + 256, s) != cudaSuccess) {
@@ -1342,7 +1375,40 @@ int filtered_index(rf_plan* p, rf_table* T, const RfParams& P, cudaStream_t s, R
     out->slots = (const long long*)*buf;
     out->cap = cap;
     out->special = (const long long*)Q.aux1;
+    // keep it for the next run: the plan's previous index and, over the context's budget, the
+    // indexes of the plans used longest ago are released in stream order after their last runs
+    const size_t bytes = cap * 16 + 256;
+    if (bytes > ctx->ixf_budget) return RF_OK;  // not kept: the caller releases it after this run
+    if (!p->ixf_ev && cudaEventCreateWithFlags(&p->ixf_ev, cudaEventDisableTiming) != cudaSuccess) {
+        p->ixf_ev = nullptr;
+        return RF_OK;
+    }
+    release_filtered_index(p, s);
+    while (ctx->ixf_bytes + bytes > ctx->ixf_budget && !ctx->ixf_lru.empty())
+        release_filtered_index(ctx->ixf_lru.front(), s);
+    p->ixf_buf = *buf;
+    p->ixf_buf_bytes = bytes;
+    p->ixf_buf_for = T->gen;
+    p->ixf_ix = *out;
+    ctx->ixf_bytes += bytes;
+    ctx->ixf_lru.push_back(p);
+    *buf = nullptr;
     return RF_OK;
+}
+
+// Releases the filtered index plan p keeps (caller holds ctx->ixf_mu): freed on s once p's last
+// run that read it is done.
+void release_filtered_index(rf_plan* p, cudaStream_t s)
+{
+    rf_ctx* ctx = p->ctx;
+    if (!p->ixf_buf) return;
+    if (p->ixf_ev) cudaStreamWaitEvent(s, p->ixf_ev, 0);
+    cudaFreeAsync(p->ixf_buf, s);
+    ctx->ixf_bytes -= p->ixf_buf_bytes;
+    ctx->ixf_lru.remove(p);
+    p->ixf_buf = nullptr;
+    p->ixf_buf_bytes = 0;
+    p->ixf_buf_for = 0;
 }
 
 int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams* Pout)
@@ -1357,7 +1423,9 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
     int units = units_for(p, ntiles);
     P.nunits = units;
     void* ixbuf = nullptr;
+    std::unique_lock<std::mutex> ixf_lock(ctx->ixf_mu, std::defer_lock);
     if (pl.ixf_input >= 0) {
+        ixf_lock.lock();
         RfTab& tab = P.t[pl.table_slot[pl.ixf_input]];
         if ((rc = filtered_index(p, args[pl.ixf_input].table, P, s, &tab.ix, &ixbuf))) {
             if (ixbuf) cudaFreeAsync(ixbuf, s);
@@ -1378,6 +1446,8 @@ int enqueue(rf_plan* p, const rf_arg* args, int n_args, cudaStream_t s, RfParams
         rc = launch(ctx, p->fns[i], grid, k.threads, k.smem, s, &P);
     }
     if (ixbuf) cudaFreeAsync(ixbuf, s);  // after the kernels that read it, in stream order
+    if (p->ixf_buf && ixf_lock.owns_lock()) cudaEventRecord(p->ixf_ev, s);  // the kept index's last use
+    if (ixf_lock.owns_lock()) ixf_lock.unlock();
     if (rc) return rc;
     if (Pout) *Pout = P;
     return RF_OK;
@@ -1456,7 +1526,9 @@ int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<H
     }
     cudaStream_t cs = ctx->copy_stream;
     void* ixbuf = nullptr;
+    std::unique_lock<std::mutex> ixf_lock(ctx->ixf_mu, std::defer_lock);
     if (pl.ixf_input >= 0) {
+        ixf_lock.lock();
         RfTab& tab = P.t[pl.table_slot[pl.ixf_input]];
         rc = filtered_index(p, args[pl.ixf_input].table, P, s, &tab.ix, &ixbuf);
     }
@@ -1502,6 +1574,8 @@ int run_streamed(rf_plan* p, const rf_arg* args, int n_args, const std::vector<H
         r0 = r1;
     }
     if (ixbuf) cudaFreeAsync(ixbuf, s);
+    if (p->ixf_buf && ixf_lock.owns_lock()) cudaEventRecord(p->ixf_ev, s);  // the kept index's last use
+    if (ixf_lock.owns_lock()) ixf_lock.unlock();
     if (rc) {
         // no copy may outlive the call (the caller owns the host memory), and the units that did
         // run left the merge ticket part-way
@@ -1950,9 +2024,11 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
     // columns are then allocated at exactly that size before the scatter, so an output holds its
     // rows, not the loop's range (a hash group-by's slot table is ~2.2x the distinct keys).  A
     // vectorised one writes every visited element and is allocated at the range up front.
+    // (a union merge knows its row count only after its scan, vectorised or not)
+    const bool union_merge = pl.kind == rfg::PlanKind::UNION_MERGE;
     int iscatter = -1;
     for (size_t i = 0; i < pl.kernels.size(); i++)
-        if (pl.kernels[i].role == rfg::KernelSpec::SCATTER && !pl.vectorize) iscatter = (int)i;
+        if (pl.kernels[i].role == rfg::KernelSpec::SCATTER && (!pl.vectorize || union_merge)) iscatter = (int)i;
     if (iscatter < 0 && (rc = alloc_cols(cap))) {
         free_table_mem(t.get());
         return rc;
@@ -1983,6 +2059,23 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         }
         P.aux4 = p->seg_woff;
         P.aux5 = p->seg_part;
+    }
+    if (union_merge) {
+        // paired-row counts of the first vector, scanned in place (nA + 1 entries)
+        rf_table* ta = args[pl.union_inputs[0]].table;
+        rf_table* tb = args[pl.union_inputs[1]].table;
+        if (!pl.vectorize && (ta->cols[0].valid || tb->cols[0].valid)) {
+            free_table_mem(t.get());
+            return fail(ctx, RF_ERR_UNSUPPORTED,
+                        "a union over iterator columns with nulls is lowered in the vectorised form only");
+        }
+        nruns = ta->cols[0].nvals + 1;
+        if (!grow((void**)&p->seg_woff, &p->seg_runs_cap, (size_t)(nruns + 1) * 8, s) ||
+            !grow((void**)&p->seg_tmp, &p->seg_tmp_cap, (size_t)(nruns / 2048 + 4) * 8, s)) {
+            free_table_mem(t.get());
+            return fail(ctx, RF_ERR_OOM, "union merge buffers");
+        }
+        P.aux4 = p->seg_woff;
     }
     int units = units_for(p, ntiles);
     P.nunits = units;
@@ -2049,7 +2142,7 @@ int run_table(rf_plan* p, const rf_arg* args, int n_args, rf_table** out, cudaSt
         return rc;
     }
     long long rows = res[0];
-    if (pl.vectorize) {
+    if (pl.vectorize && !union_merge) {
         long long a = std::max(lo, rng[0]), b = std::min(hi, rng[1]);
         rows = b > a ? b - a : 0;
     }

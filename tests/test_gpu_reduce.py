@@ -173,3 +173,23 @@ def test_groupby_mixed_signs_wide_exponents(eng):
     got = plan.run(dt)
     assert_same(got, loopgen.Query(fn)(t))
     assert plan.run(dt) == got  # same bits on a second run
+
+
+def test_join_filtered_index_kept_between_runs(eng):
+    # a plan keeps its filtered index for the next run on the same table (same bits), and a new
+    # upload of the build side (a new table generation) is never answered from the kept index
+    b, p = W.join_tables(50_000, 400_001, seed=61)
+    fn = W.join_query(b.get_data_type(), p.get_data_type())
+    plan = eng.compile(fn)
+    db, dp = eng.upload(b), eng.upload(p)
+    first = plan.run(db, dp)
+    assert plan.run(db, dp) == first
+    assert_same(first, loopgen.Query(fn)(b, p))
+    rng = np.random.default_rng(62)
+    b.columns[1].data = rng.permutation(b.columns[1].data)  # other rows pass the build filter now
+    db2 = eng.upload(b)
+    again = plan.run(db2, dp)
+    assert_same(again, loopgen.Query(fn)(b, p))
+    assert again != first
+    # back on the first table: its own answer, not the one the kept index would give
+    assert plan.run(db, dp) == first
