@@ -364,12 +364,17 @@ def measure_config(eng, wl: Workload, config: int, args, rank: int, world: int, 
     out_rows = [0]
     last = [None]
     tuning = {}
-    # the autotuner picks the scan tile (or the hash table's sizing) for this shape and size
-    # once, before warm-up (rf_plan_tune; every later run of the shape uses it)
-    if not table_out and plan.kind in (1, 2):
+    # the autotuner picks the block size and scan tile (or the hash table's sizing) for this
+    # shape and size once, before warm-up (rf_plan_tune; every later run of the shape uses it)
+    if args.tune_file:
+        tuning["from_file"] = args.tune_file
+    elif not table_out and plan.kind in (1, 2):
         tuning["tile_rows"], _ = plan.tune(*dts, reps=3)
+        tuning["block"] = next((m for m in (128, 256, 512) if "_KERNEL(rf_main, %d)" % m in plan.source), None)
     elif plan.kind == 5:
         tuning["hash_slots_per_100_keys"], _ = plan.tune(*dts, reps=2)
+    if args.save_tune:
+        eng.tune_save(args.save_tune)
 
     def step(keep=False):
         if not table_out:
@@ -705,6 +710,10 @@ def main():
                     help="table-result queries the batched server runs at once (0: the server's default)")
     ap.add_argument("--serving-table-priority", type=int, default=0,
                     help="the batched server's table lanes: >= 0 highest stream priority (default), < 0 normal")
+    ap.add_argument("--save-tune", default="",
+                    help="write the autotuner's choices to this JSON file after tuning")
+    ap.add_argument("--tune-file", default="",
+                    help="take the autotuner's choices from this JSON file instead of tuning (profiling runs)")
     ap.add_argument("--ingest", action="store_true",
                     help="measure Arrow IPC ingest of the config's table instead (one JSON line)")
     ap.add_argument("--serving-only", action="store_true",
@@ -732,6 +741,8 @@ def main():
     from reffine_gb300 import engine
     dist = Dist(world)
     eng = engine.Engine(local)
+    if args.tune_file:
+        eng.tune_load(args.tune_file)  # compiles below take the file's block sizes and tilings
     wl = build_workload(args.config, rank, world, args.rows)
     head = measure_config(eng, wl, args.config, args, rank, world, dist, cpu=not args.no_cpu)
     del wl

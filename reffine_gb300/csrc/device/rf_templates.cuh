@@ -81,34 +81,37 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
     __syncthreads();
     if (last) {
         __threadfence();
-        if (warp == 0) {
-            // units lane, lane+32, ... folded in that order; their loads are issued RF_FOLD_ACC
-            // at a time ahead of the combines
-            RfAcc tot;
-            rf_acc_init(P, tot);
-            int u = lane;
-            for (; u + 32 * (RF_FOLD_ACC - 1) < nunits; u += 32 * RF_FOLD_ACC) {
-                RfAcc v[RF_FOLD_ACC];
+        // the whole block folds the units' partials: thread t takes units t, t+T, t+2T, ... in
+        // that order (their loads issued RF_FOLD_ACC at a time ahead of the combines), then the
+        // lanes of each warp by shuffles and the warps in order - a fixed order on every path
+        RfAcc tot;
+        rf_acc_init(P, tot);
+        int u = threadIdx.x;
+        for (; u + T * (RF_FOLD_ACC - 1) < nunits; u += T * RF_FOLD_ACC) {
+            RfAcc v[RF_FOLD_ACC];
 #pragma unroll
-                for (int k = 0; k < RF_FOLD_ACC; k++)
-                    rf_ld_words(&v[k], (const RfAcc*)P.partials + u + 32 * k, (int)sizeof(RfAcc));
+            for (int k = 0; k < RF_FOLD_ACC; k++)
+                rf_ld_words(&v[k], (const RfAcc*)P.partials + u + T * k, (int)sizeof(RfAcc));
 #pragma unroll
-                for (int k = 0; k < RF_FOLD_ACC; k++) rf_acc_combine(tot, v[k]);
-            }
-            for (; u < nunits; u += 32) {
-                RfAcc p;
-                rf_ld_words(&p, (const RfAcc*)P.partials + u, (int)sizeof(RfAcc));
-                rf_acc_combine(tot, p);
-            }
+            for (int k = 0; k < RF_FOLD_ACC; k++) rf_acc_combine(tot, v[k]);
+        }
+        for (; u < nunits; u += T) {
+            RfAcc p;
+            rf_ld_words(&p, (const RfAcc*)P.partials + u, (int)sizeof(RfAcc));
+            rf_acc_combine(tot, p);
+        }
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                RfAcc o = rf_acc_shfl(tot, off);
-                rf_acc_combine(tot, o);
-            }
-            if (lane == 0) {
-                rf_finish(P, tot, P.out);
-                *P.counter = 0u;
-            }
+        for (int off = 16; off > 0; off >>= 1) {
+            RfAcc o = rf_acc_shfl(tot, off);
+            rf_acc_combine(tot, o);
+        }
+        if (lane == 0) warp_acc[warp] = tot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            RfAcc all = warp_acc[0];
+            for (int w = 1; w < T / 32; w++) rf_acc_combine(all, warp_acc[w]);
+            rf_finish(P, all, P.out);
+            *P.counter = 0u;
         }
     }
     __syncthreads();  // shared state is reused by the next work item of a persistent block

@@ -241,11 +241,15 @@ struct Space {
 
 class Lowerer {
 public:
-    Lowerer(std::shared_ptr<Func> fn, bool vectorize) : fn_(std::move(fn)), vectorize_(vectorize) {}
+    Lowerer(std::shared_ptr<Func> fn, bool vectorize, int threads)
+        : fn_(std::move(fn)), vectorize_(vectorize), threads_(threads)
+    {
+    }
 
     Plan run()
     {
         plan_.vectorize = vectorize_;
+        plan_.threads = threads_;
         plan_.n_inputs = (int)fn_->inputs.size();
         int tslot = 0, sslot = 0;
         for (size_t i = 0; i < fn_->inputs.size(); i++) {
@@ -3221,6 +3225,7 @@ extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_con
 
     std::shared_ptr<Func> fn_;
     bool vectorize_;
+    int threads_;
     Plan plan_;
     std::map<const ExprNode*, int> input_index_;
 };
@@ -3251,6 +3256,10 @@ size_t c_size(const DataType& t)
     return t.size();
 }
 
-Plan lower(const std::shared_ptr<Func>& fn, bool vectorize) { return Lowerer(fn, vectorize).run(); }
+Plan lower(const std::shared_ptr<Func>& fn, bool vectorize, int threads)
+{
+    if (threads != 128 && threads != 256 && threads != 512) throw LowerError("block size must be 128, 256 or 512");
+    return Lowerer(fn, vectorize, threads).run();
+}
 
 }  // namespace rfg

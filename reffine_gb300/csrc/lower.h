@@ -94,7 +94,9 @@ struct Plan {
     bool vectorize = false;
 };
 
-Plan lower(const std::shared_ptr<Func>& fn, bool vectorize);
+// `threads`: the block size of the scan templates' kernels (128, 256 or 512; the autotuner
+// chooses it per query shape)
+Plan lower(const std::shared_ptr<Func>& fn, bool vectorize, int threads = 256);
 
 // hash group-by: slots of the shared-memory hot-key table per hot key (a power of two)
 constexpr int kHotSlotsPerKey = 16;

@@ -157,6 +157,8 @@ struct rf_table {
 
 struct rf_plan {
     rf_ctx* ctx = nullptr;
+    std::string text;                 // the Func's text (the autotuner recompiles variants from it)
+    std::string shape;                // shape key at the default block size (tuning entries)
     std::vector<rf_table*> staging;   // device copies of the host tables of thunk calls
     rfg::Plan plan;
     std::shared_ptr<JitModule> mod;

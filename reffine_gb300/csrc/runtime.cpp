@@ -997,16 +997,16 @@ static int unit_waves(const rfg::Plan& pl)
     return 1;
 }
 
-extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_plan** out)
+namespace {
+// The plan of `fn` at block size `threads`: lowered, its kernels compiled and loaded, its work
+// units sized and its device buffers allocated (rf_plan_compile, and the autotuner's variants).
+int build_plan(rf_ctx* ctx, const std::shared_ptr<reffine::Func>& fn, bool vectorize, int threads,
+               std::unique_ptr<rf_plan>& p)
 {
-    if (!ctx || !text || !out) return fail(ctx, RF_ERR_INVALID, "null argument");
-    *out = nullptr;
-    cudaSetDevice(ctx->device);
-    auto p = std::make_unique<rf_plan>();
+    p = std::make_unique<rf_plan>();
     p->ctx = ctx;
     try {
-        auto fn = reffine::parse_text(text);
-        p->plan = rfg::lower(fn, vectorize != 0);
+        p->plan = rfg::lower(fn, vectorize, threads);
     } catch (const rfg::LowerError& e) {
         return fail(ctx, e.unsupported ? RF_ERR_UNSUPPORTED : RF_ERR_INVALID, "%s", e.what());
     } catch (const std::exception& e) {
@@ -1089,6 +1089,40 @@ extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_
     }
     CUDA_TRY(ctx, cudaMemsetAsync(p->counter, 0, 64, ctx->stream));
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // ready for use on any stream
+    return RF_OK;
+}
+}  // namespace
+
+extern "C" int rf_plan_compile(rf_ctx* ctx, const char* text, int vectorize, rf_plan** out)
+{
+    if (!ctx || !text || !out) return fail(ctx, RF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    std::shared_ptr<reffine::Func> fn;
+    std::string shape;
+    try {
+        fn = reffine::parse_text(text);
+        shape = rfg::lower(fn, vectorize != 0).key;  // the query shape at the default block size
+    } catch (const rfg::LowerError& e) {
+        return fail(ctx, e.unsupported ? RF_ERR_UNSUPPORTED : RF_ERR_INVALID, "%s", e.what());
+    } catch (const std::exception& e) {
+        return fail(ctx, RF_ERR_INVALID, "%s", e.what());
+    }
+    // a block size the autotuner chose for this shape (kept as bucket -1 of the shape's entry)
+    int threads = 256;
+    {
+        std::lock_guard<std::mutex> g(ctx->tune_mu);
+        auto it = ctx->tune.find(shape);
+        if (it != ctx->tune.end()) {
+            auto jt = it->second.find(-1);
+            if (jt != it->second.end()) threads = (int)jt->second;
+        }
+    }
+    std::unique_ptr<rf_plan> p;
+    int rc = build_plan(ctx, fn, vectorize != 0, threads, p);
+    if (rc) return rc;
+    p->text = text;
+    p->shape = shape;
     *out = p.release();
     return RF_OK;
 }
@@ -1662,6 +1696,10 @@ static int tune_hash_table(rf_plan* p, const rf_arg* args, int n_args, int reps,
     return RF_OK;
 }
 
+namespace {
+int tune_block_and_tiles(rf_plan* p, const rf_arg* args, int32_t n_args, int32_t reps, int64_t* tile_rows, double* ms);
+}
+
 extern "C" int rf_plan_tune(rf_plan* p, const rf_arg* args, int32_t n_args, int32_t reps, int64_t* tile_rows,
                             double* ms)
 {
@@ -1673,7 +1711,18 @@ extern "C" int rf_plan_tune(rf_plan* p, const rf_arg* args, int32_t n_args, int3
     if (pl.kind == rfg::PlanKind::HASH_GROUP) return tune_hash_table(p, args, n_args, reps, tile_rows, ms);
     if (pl.out_is_table || (pl.kind != rfg::PlanKind::SCAN_REDUCE && pl.kind != rfg::PlanKind::GROUP_REDUCE))
         return fail(ctx, RF_ERR_UNSUPPORTED,
-                    "the autotuner tunes the tiling of Reduce scans and the table sizing of hash group-bys");
+                    "the autotuner tunes the block size and tiling of Reduce scans and the table sizing of hash "
+                    "group-bys");
+    return tune_block_and_tiles(p, args, n_args, reps, tile_rows, ms);
+}
+
+namespace {
+// the tiling of a Reduce scan at the plan's current kernels: tiles of 1K..32K rows timed on the
+// given inputs, the fastest recorded for the plan's shape key and the inputs' size bucket
+int tune_tiles(rf_plan* p, const rf_arg* args, int32_t n_args, int32_t reps, int64_t* tile_rows, double* ms)
+{
+    rf_ctx* ctx = p->ctx;
+    const rfg::Plan& pl = p->plan;
     RfParams P;
     long long lo, hi;
     int rc = fill_params(p, args, n_args, P, lo, hi, true);
@@ -1685,9 +1734,18 @@ extern "C" int rf_plan_tune(rf_plan* p, const rf_arg* args, int32_t n_args, int3
     CUDA_TRY(ctx, cudaEventCreate(&e1));
     long long best = 0;
     float best_ms = 0;
-    // candidate tilings from 1K rows to 32K rows (no tile much larger than the input)
-    for (long long t = 1024; t <= 32768; t *= 2) {
-        if (t > 2 * rows && best) break;
+    // candidate tilings: 1K to 32K rows (no tile much larger than the input), and the tiles that
+    // cut the rows into 1-4 whole waves of resident blocks (no partly filled last wave); a
+    // multiple of 4 rows, so a tile starts where 4-row vector loads do
+    std::vector<long long> cand;
+    for (long long t = 1024; t <= 32768; t *= 2)
+        if (t <= 2 * rows || cand.empty()) cand.push_back(t);
+    for (int w = 1; w <= 4 && p->max_units > 0; w++) {
+        const long long units = (long long)p->max_units * w;
+        const long long t = ((rows + units - 1) / units + 3) & ~3LL;
+        if (t >= 256 && t <= 65536 && std::find(cand.begin(), cand.end(), t) == cand.end()) cand.push_back(t);
+    }
+    for (long long t : cand) {
         p->tile_override = t;
         std::vector<float> v;
         for (int r = 0; r <= reps && !rc; r++) {
@@ -1723,6 +1781,84 @@ extern "C" int rf_plan_tune(rf_plan* p, const rf_arg* args, int32_t n_args, int3
     return RF_OK;
 }
 
+// The plan's kernels and the buffers shaped by them, exchanged with a variant's (the variant
+// then holds, and frees, the plan's former ones).
+void swap_kernels(rf_plan* a, rf_plan* b)
+{
+    std::swap(a->plan, b->plan);
+    std::swap(a->mod, b->mod);
+    std::swap(a->fns, b->fns);
+    std::swap(a->buf, b->buf);
+    std::swap(a->partials, b->partials);
+    std::swap(a->partials_bytes, b->partials_bytes);
+    std::swap(a->counter, b->counter);
+    std::swap(a->range, b->range);
+    std::swap(a->dout, b->dout);
+    std::swap(a->max_units, b->max_units);
+    std::swap(a->reduce_units, b->reduce_units);
+    std::swap(a->batch_fn, b->batch_fn);
+    std::swap(a->batch_grid, b->batch_grid);
+    std::swap(a->batch_smem, b->batch_smem);
+    std::swap(a->batch_threads, b->batch_threads);
+}
+
+// Block size and tiling together: the plan's shape compiled at 128, 256 and 512 threads per block
+// (a variant that cannot be resident is skipped), each variant's tiling tuned, and the fastest
+// pair kept - the plan takes that variant's kernels, and later compiles of the same shape in
+// this context start from that block size.  Results then come from the chosen kernels on every
+// path (alone, batched, served), so they stay the same everywhere.
+int tune_block_and_tiles(rf_plan* p, const rf_arg* args, int32_t n_args, int32_t reps, int64_t* tile_rows, double* ms)
+{
+    rf_ctx* ctx = p->ctx;
+    int64_t best_tile = 0;
+    double best_ms = 0;
+    int best_threads = p->plan.threads;
+    std::unique_ptr<rf_plan> best_variant;
+    int rc = tune_tiles(p, args, n_args, reps, &best_tile, &best_ms);
+    if (rc) return rc;
+    if (!p->text.empty()) {
+        std::shared_ptr<reffine::Func> fn;
+        try {
+            fn = reffine::parse_text(p->text);
+        } catch (const std::exception& e) {
+            return fail(ctx, RF_ERR_INVALID, "%s", e.what());
+        }
+        for (int threads : {128, 256, 512}) {
+            if (threads == p->plan.threads) continue;
+            std::unique_ptr<rf_plan> v;
+            if (build_plan(ctx, fn, p->plan.vectorize, threads, v)) {
+                if (v) rf_plan_free(v.release());
+                continue;  // e.g. too much shared memory at this block size
+            }
+            int64_t t = 0;
+            double m = 0;
+            if (tune_tiles(v.get(), args, n_args, reps, &t, &m) == RF_OK && m < best_ms) {
+                best_tile = t;
+                best_ms = m;
+                best_threads = threads;
+                if (best_variant) rf_plan_free(best_variant.release());
+                best_variant = std::move(v);
+            } else {
+                rf_plan_free(v.release());
+            }
+        }
+        cudaGetLastError();
+    }
+    if (best_variant) {
+        cudaStreamSynchronize(ctx->stream);
+        swap_kernels(p, best_variant.get());
+        rf_plan_free(best_variant.release());
+    }
+    if (!p->shape.empty()) {
+        std::lock_guard<std::mutex> g(ctx->tune_mu);
+        ctx->tune[p->shape][-1] = best_threads;
+    }
+    if (tile_rows) *tile_rows = best_tile;
+    if (ms) *ms = best_ms;
+    return RF_OK;
+}
+}  // namespace
+
 extern "C" int rf_tune_export(rf_ctx* ctx, char* buf, size_t len, size_t* needed)
 {
     if (!ctx) return RF_ERR_INVALID;
@@ -1751,7 +1887,9 @@ extern "C" int rf_tune_import(rf_ctx* ctx, const char* text)
     long long tile;
     std::map<std::string, std::map<int, long long>> add;
     while (in >> key >> bucket >> tile) {
-        if (bucket < 0 || bucket > 62 || tile < 32 || tile > (1LL << 30))
+        const bool block = bucket == -1;  // the shape's block size
+        if (block ? (tile != 128 && tile != 256 && tile != 512)
+                  : (bucket < 0 || bucket > 62 || tile < 32 || tile > (1LL << 30)))
             return fail(ctx, RF_ERR_INVALID, "tuning entry %s %d %lld out of range", key.c_str(), bucket, tile);
         add[key][bucket] = tile;
     }

@@ -19,7 +19,10 @@ def test_tune_filter_sum_and_groupby(eng, tmp_path):
     plan = eng.compile(W.filter_sum_query(t.get_data_type(), 700, 1300))
     before = plan.run(dt)
     tile, ms = plan.tune(dt, reps=3)
-    assert tile in (1024, 2048, 4096, 8192, 16384, 32768) and ms > 0
+    assert tile % 4 == 0 and 256 <= tile <= 65536 and ms > 0
+    # the block size chosen with it: kept for the shape (bucket -1) and used by the plan's kernels
+    blocks = [int(l.split()[2]) for l in eng.tune_export().splitlines() if l.split()[1] == "-1"]
+    assert blocks and all(b in (128, 256, 512) for b in blocks)
     after = plan.run(dt)
     ref = loopgen.Query(plan.fn)(t)
     assert_same(after, ref)
@@ -31,6 +34,9 @@ def test_tune_filter_sum_and_groupby(eng, tmp_path):
     b.launch()
     got = b.wait()
     assert got[0] == after and got[1] == other.run(dt)
+    block = [m for m in (128, 256, 512) if "RF_SCAN_REDUCE_KERNEL(rf_main, %d)" % m in plan.source]
+    assert len(block) == 1 and "RF_SCAN_REDUCE_KERNEL(rf_main, %d)" % block[0] in other.source
+    assert_same(other.run(dt), loopgen.Query(other.fn)(t))
     text = eng.tune_export()
     assert str(tile) in text and len(text.splitlines()) >= 1
     g = W.groupby_table(1_000_003, seed=42)
