@@ -8,7 +8,8 @@ line each.
 REFFINE_SRC is a checkout of Reffine.  The test program (tests/ref_binding/ref_queries.cpp) is
 compiled with g++ together with the binding (reffine_gb300/binding/ref_binding.cpp) and the
 reference's LLVM-free IR sources: src/builder/reffiner.cpp, src/base/type.cpp and src/ir/ir.cpp,
-the last with tests/ref_binding/shim ahead on the include path (its printer2.h needs LLVM).
+the last with oracle/ref/shim ahead on the include path (its printer2.h needs LLVM).  The queries
+themselves are in oracle/ref/ref_queries.h, shared with the reference-pipeline oracle.
 """
 import os
 import subprocess
@@ -24,7 +25,8 @@ def build_and_run(src: str) -> str:
     os.makedirs(out_dir, exist_ok=True)
     exe = os.path.join(out_dir, "ref_queries")
     cmd = ["g++", "-std=c++20", "-O1",
-           "-I", os.path.join(ROOT, "tests", "ref_binding", "shim"),
+           "-I", os.path.join(ROOT, "oracle", "ref", "shim"),
+           "-I", os.path.join(ROOT, "oracle", "ref"),
            "-I", os.path.join(src, "include"),
            "-I", os.path.join(ROOT, "include"),
            os.path.join(ROOT, "tests", "ref_binding", "ref_queries.cpp"),

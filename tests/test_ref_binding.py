@@ -48,6 +48,7 @@ def python_funcs():
         "groupby": W.groupby_query(W.groupby_table(8).get_data_type()),
         "hashgroup": W.hashgroup_query(W.hashgroup_table(8, 4).get_data_type()),
         "join_agg": W.join_query(b.get_data_type(), p.get_data_type()),
+        "hashgroup_ree": W.hashgroup_query(W.ree_sorted(W.hashgroup_table(8, 4)).get_data_type()),
     }
 
 
