@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Benchmark: compiled Reffine query on one GB300, against the oracle port on the host cores.
+"""Benchmark: compiled Reffine query on one GB300, against Reffine's own code on the host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1] [--impl ours|reference]
 
@@ -12,7 +12,9 @@ GB/s = algorithmic bytes (each referenced column read once) / time.
              pointer: ArrowTable* in, result out), host tables in pinned memory, host->device
              copies of the referenced columns and the device->host result copy inside the timing
   roofline   achieved algorithmic GB/s of the main kernel against the measured HBM copy peak
-  cpu_baseline  the oracle (Reffine's CPU loop restated, g++ -O3, one core) on the same table
+  cpu_baseline  Reffine's own emitted C++ for the query (oracle/ref/generated, g++ -O3) on the
+             same table: one copy per host thread at once (value) and one thread alone; the
+             oracle port's one-core figure beside it
   parity     the GPU result against the oracle's on the same full-size tables: integers
              bit-exact, FP64 max relative error (the bar is 1e-12)
   per_config the same measurements (value, roofline, e2e, cpu_baseline, parity) for the other
@@ -21,8 +23,9 @@ GB/s = algorithmic bytes (each referenced column read once) / time.
              continuous-batching server against per-query launches on the same GPU (p50/p99
              latency, queries/s, GB/s), every result checked against the query run alone
 
---impl reference times the oracle port alone (the reference's CPU path; it is single-threaded);
-it counts bytes from the columns each workload declares and loads nothing of the GPU backend.
+--impl reference times Reffine's emitted code alone on every host thread (the reference's CPU
+path runs a query serially, so one copy per thread); it counts bytes from the columns each
+workload declares and loads nothing of the GPU backend.
 Multi-GPU (torchrun): each rank scans its own partition (weak scaling; a join's build side is
 the same on every rank), no collective on the data path; rank 0 prints the max-over-ranks time.
 After the timed steps each rank's partial state is gathered to rank 0 and folded in rank order
@@ -209,6 +212,70 @@ def reference_form(config, fn, tables):
     return W.hashgroup_query(ree.get_data_type()), [ree]
 
 
+GENERATED = {0: "filter_sum", 1: "groupby", 2: "hashgroup_ree", 3: "join_agg"}
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reffine_code(config, fn, tables):
+    """Reffine's own emitted C++ for this workload's query (oracle/ref/generated, compiled with
+    g++ -O3 and the compiler's default contraction), its tables prepared (Locate indexes built)."""
+    from oracle import ref_generated
+    q = ref_generated.GeneratedQuery(GENERATED[config], fn)
+    q.prepare(*tables)
+    return q
+
+
+def reffine_code_sample(config, fn, tables, target_s):
+    """Reffine's emitted code prepared on a bounded sample of the workload: the driving (last)
+    table cut to a row prefix whose one-thread run takes about target_s seconds, or whole when it
+    takes less (a run-end table is always whole).  (query, fraction of rows, one-thread seconds,
+    one-thread result.)"""
+    d = tables[-1]
+    q = None
+    if len(d) >= 64 and all(c.run_ends is None for c in d.columns):
+        probe = len(d) // 64
+        q = reffine_code(config, fn, tables[:-1] + [d.rows(0, probe)])
+        t_small, _ = q.run(1)
+        est = t_small * len(d) / probe
+        if est > target_s:
+            n = max(probe, int(len(d) * target_s / est))
+            q.prepare(*(tables[:-1] + [d.rows(0, n)]))
+            t1, r1 = q.run(1)
+            return q, n / len(d), t1, r1[0]
+        q.prepare(*tables)
+    if q is None:
+        q = reffine_code(config, fn, tables)
+    t1, r1 = q.run(1)
+    return q, 1.0, t1, r1[0]
+
+
+def reffine_code_run(config, fn, tables, nbytes, note="", target_s=4.0):
+    """Reffine's emitted code on the host cores: one query on one thread (Reffine runs a query
+    serially), then one copy of the query on every host thread at once, on a bounded sample.
+    (cpu_baseline dict, the one-thread result on the whole table or None for a sample.)"""
+    q, frac, t1, r1 = reffine_code_sample(config, fn, tables, target_s)
+    nthr = host_threads()
+    tn, rn = q.run(nthr)
+    q.release()
+    agree = all(repr(r) == repr(r1) for r in rn) if not isinstance(r1, dict) else \
+        all(r["len"] == r1["len"] for r in rn)
+    kind = platform.processor() or platform.machine()
+    b = nbytes * frac
+    what = "the full table" if frac == 1.0 else "the first %.2f%% of the driving table's rows" % (100 * frac)
+    base = {"value": nthr * b / tn / 1e9, "unit": "GB/s", "cores": nthr, "kind": "reference",
+            "sample": "Reffine's emitted code for the query (LoopGen..CEmitter output, g++ -O3) on %s: %d copies "
+                      "at once, one per host thread, %.3f s; %s%s" % (what, nthr, tn, kind, note),
+            "single_thread": {"value": b / t1 / 1e9, "seconds": t1},
+            "threads_agree": agree}
+    return base, (r1 if frac == 1.0 else None)
+
+
 def oracle_run(fn, tables, nbytes, budget_s=20.0, note=""):
     """The oracle port (Reffine's serial loop restated, g++ -O3, one core) on the same tables:
     (cpu_baseline dict, seconds per run, the result of the first run)."""
@@ -293,39 +360,36 @@ def table_parity(out, ref, values=None, keys=None) -> dict:
 
 
 def run_reference(args, rank, world):
-    """The reference's CPU path for the same workload: the oracle port of Reffine's generated
-    serial loop, one core (the reference's generated code is single-threaded).  Counts bytes from
-    the workload's declared columns; loads nothing of the GPU backend."""
+    """The reference's CPU path for the same workload: the C++ Reffine's own compile path emits
+    for the query (oracle/ref/generated; g++ -O3), on every host thread.  Reffine runs one query
+    serially, so a step runs one copy of the whole query per host thread at once and the value is
+    the bytes all copies scanned over the step's wall time; the single-thread figure is reported
+    beside it.  Counts bytes from the workload's declared columns; loads nothing of the GPU
+    backend."""
     if rank != 0:
         return 0
     wl = build_workload(args.config, 0, 1, args.rows)
     nbytes = wl.algorithmic_bytes()
     fn, tables = reference_form(args.config, wl.fn, wl.tables)
-    from oracle import loopgen
-    q = loopgen.Query(fn)
-    table_out = fn.output.type.is_vector()
-
-    def once():
-        out, cargs = q.prepare(*tables)
-        t0 = time.perf_counter()
-        q.run_prepared(out, cargs)
-        dt = time.perf_counter() - t0
-        if table_out:
-            q.result(out)
-        return dt
-
+    # each step a bounded sample: the driving table's first rows, about 2 s of one thread's work
+    q, frac, t1, _ = reffine_code_sample(args.config, fn, tables, 2.0)
+    nthr = host_threads()
     for _ in range(args.warmup):
-        once()
-    times = [once() for _ in range(args.steps)]
+        q.run(nthr)
+    times = [q.run(nthr)[0] for _ in range(args.steps)]
+    q.release()
     sec = float(np.mean(times))
-    val = nbytes / sec / 1e9
+    nbytes = nbytes * frac
+    val = nthr * nbytes / sec / 1e9
+    what = "the whole table" if frac == 1.0 else "the first %.2f%% of the driving table's rows" % (100 * frac)
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": wl.name, **wl.cfg, "l2": L2_NOTE},
-            "cpu_baseline": {"value": val, "unit": "GB/s", "cores": 1, "kind": "port",
-                             "sample": "the full table per step (Reffine's serial loop restated, g++ -O3, "
-                                       "one core)"},
+            "cpu_baseline": {"value": val, "unit": "GB/s", "cores": nthr, "kind": "reference",
+                             "sample": "per step, one copy of the query over %s per host thread at once (%d), "
+                                       "Reffine's emitted code compiled with g++ -O3" % (what, nthr),
+                             "single_thread": {"value": nbytes / t1 / 1e9, "seconds": t1}},
             "e2e": {"value": val, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "algorithmic_bytes_per_step": nbytes}
     print(json.dumps(line), flush=True)
@@ -494,16 +558,21 @@ def measure_config(eng, wl: Workload, config: int, args, rank: int, world: int, 
 
     if cpu and rank == 0:
         rfn, rtabs = reference_form(config, wl.fn, wl.tables)
-        base, _, ref = oracle_run(rfn, rtabs, nbytes, note="" if config != 2 else
-                                  "; keys pre-sorted and run-end encoded (the reference's grouped form), sort not "
-                                  "timed")
+        note = "" if config != 2 else \
+            "; keys pre-sorted and run-end encoded (the reference's grouped form), sort not timed"
+        port, _, ref = oracle_run(rfn, rtabs, nbytes, note=note)
+        base, rcode = reffine_code_run(config, rfn, rtabs, nbytes, note=note)
+        base["oracle_port"] = {"value": port["value"], "cores": 1}
         res["cpu_baseline"] = base
         if table_out:
-            res["parity"] = table_parity(got, ref, values=wl.tables[0].columns[1].data,
-                                         keys=wl.tables[0].columns[0].data)
+            kw = dict(values=wl.tables[0].columns[1].data, keys=wl.tables[0].columns[0].data)
+            res["parity"] = table_parity(got, ref, **kw)
         else:
             res["parity"] = value_parity(got, ref)
         res["parity"]["against"] = "oracle on the same full-size tables (rows %d)" % wl.rows
+        if rcode is not None:
+            res["parity_reffine_code"] = table_parity(got, rcode) if table_out else value_parity(got, rcode)
+            res["parity_reffine_code"]["against"] = "Reffine's emitted code on the same tables (default contraction)"
     else:
         res["cpu_baseline"] = None
         res["parity"] = None
