@@ -289,6 +289,92 @@ RF_DEV unsigned long long rf_f2u(double x) { return (unsigned long long)__double
 RF_DEV double rf_u2f(unsigned long long x) { return __longlong_as_double((long long)x); }
 
 // ---------------------------------------------------------------------------------------
+// FP64 sums on the FP32 pipe.  GB300's FP64 pipe issues about 1/64 of its FP32 rate, and a
+// grouped scan spends most of it on its sums.  A sum slot can instead hold an unevaluated pair of
+// floats hi + lo (a "double-float", 48 significant bits): each addend is split into two floats
+// with integer operations only, and added with the error-free two-sum of Knuth (TAOCP vol. 2,
+// 4.2.2) and Dekker's renormalisation (the accurate double-float addition of Hida, Li and Bailey's
+// QD library): the pair stays within about 2^-47 of the exact running sum, relative to the sum.
+// FP64 sums of the same rows in another order differ by the same order of rounding, far inside
+// the 1e-12 relative tolerance kept against the serial reference loop.
+// A slot's 64 bits hold the pair (hi in the low word, lo in the high word); +0.0 is all zeros in
+// both encodings.
+// ---------------------------------------------------------------------------------------
+
+// v = hi + lo, |hi + lo - v| <= 2^-47 |v|; false (and nothing set) unless v is +-0 or a normal
+// double of magnitude in [2^-103, 2^100): subnormals, larger values, infinities and NaN are left
+// to FP64 arithmetic.  hi takes the sign, the exponent and the leading 23 fraction bits of v (so
+// hi is v truncated to 24 bits); lo the next 23, rounded to nearest on the 6 bits after them,
+// built as (1.m - 1.0) x 2^k from two floats with the same exponent, which subtract exactly.
+RF_DEV bool rf_df_split(double v, float& hi, float& lo)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
+    const unsigned e = (h >> 20) & 0x7FFu;
+    if (e - 920u >= 204u) {
+        hi = 0.f;
+        lo = 0.f;
+        return (b << 1) == 0ULL;
+    }
+    const unsigned s = h & 0x80000000u;
+    hi = __uint_as_float(s | ((h - (896u << 20)) << 3) | (l >> 29));
+    const unsigned c = s | ((e - 919u) << 23);
+    lo = __uint_as_float(c + (((l & 0x1FFFFFFFu) + 32u) >> 6)) - __uint_as_float(c);
+    return true;
+}
+
+RF_DEV void rf_two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+RF_DEV void rf_quick_two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// (ah, al) += (bh, bl)
+RF_DEV void rf_df_add(float& ah, float& al, float bh, float bl)
+{
+    float s1, s2, t1, t2;
+    rf_two_sum(ah, bh, s1, s2);
+    rf_two_sum(al, bl, t1, t2);
+    s2 = __fadd_rn(s2, t1);
+    rf_quick_two_sum(s1, s2, s1, s2);
+    s2 = __fadd_rn(s2, t2);
+    rf_quick_two_sum(s1, s2, ah, al);
+}
+
+// a double-float slot += v.  False, with the slot unchanged, when v is out of the split's range,
+// when v and the sum so far have opposite signs, or when the sum would reach 2^120 (far below
+// the float range): the caller then turns its slots into doubles and adds v in FP64.  Addends of
+// one sign keep the sum well conditioned, so its relative error stays that of the additions
+// (about 2^-48 times the square root of their number, typically); a sum with cancellation is
+// left to FP64, whose error relative to the result is 32 times smaller.
+RF_DEV bool rf_df_slot_add(unsigned long long* s, double v)
+{
+    float bh, bl;
+    if (!rf_df_split(v, bh, bl)) return false;
+    const unsigned long long w = *s;
+    float ah = __uint_as_float((unsigned)w), al = __uint_as_float((unsigned)(w >> 32));
+    if (((unsigned)w ^ __float_as_uint(bh)) >> 31 && ah != 0.f && bh != 0.f) return false;
+    rf_df_add(ah, al, bh, bl);
+    if (!(fabsf(ah) < 0x1p120f)) return false;
+    *s = (unsigned long long)__float_as_uint(ah) | ((unsigned long long)__float_as_uint(al) << 32);
+    return true;
+}
+
+// the double nearest hi + lo of a double-float slot, as slot bits
+RF_DEV unsigned long long rf_df_slot_to_f64(unsigned long long w)
+{
+    const double hi = (double)__uint_as_float((unsigned)w), lo = (double)__uint_as_float((unsigned)(w >> 32));
+    return rf_f2u(__dadd_rn(hi, lo));
+}
+
+// ---------------------------------------------------------------------------------------
 // Bulk L2 prefetch (sm_90+): the copy engine pulls a contiguous byte range into L2; no
 // registers, no shared memory, nothing to wait for.  rf_pf prefetches the rows [r0, r1) of a
 // column of `size`-byte values, rounded inwards to whole 16-byte blocks, so it never touches

@@ -151,7 +151,9 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
 // Template 2: grouped scan-reduce with shared-memory privatised accumulators.
 //   The fragment defines RF_G groups x RF_M aggregates, struct RfVals, rf_group(P, r, V)
 //   (group id or -1, and the row's aggregate inputs), rf_slot_init(m) (64-bit identity),
-//   rf_slot_combine(m, a, b), rf_slot_add(S, g, t, V) and rf_finish_groups(P, tot, out).
+//   rf_slot_combine(m, a, b), rf_slot_add(S, g, t, V, df), rf_slots_done(S, t, df) (df: the
+//   thread keeps its FP64 sums as double-floats, see rf_device.cuh) and
+//   rf_finish_groups(P, tot, out).
 // Each thread owns a private column of G*M 64-bit slots in shared memory (slot (q, t) at
 // S[q * T + t]): no atomics and no bank conflicts on the per-row update.  At the end every
 // slot column is folded over the block in a fixed order, then over units by the last unit.
@@ -165,6 +167,7 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int Q = RF_G * RF_M;
     for (int q = 0; q < Q; q++) S[q * T + tid] = rf_slot_init(P, q % RF_M);
+    bool df = true;  // the thread's FP64 sum slots hold double-floats (rf_slot_add, rf_slots_done)
     long long lo = P.row_lo, hi = P.row_hi;
     if (P.range) {
         long long b = P.range[0], e = P.range[1];
@@ -211,7 +214,7 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
                 if (qn >= 32) {
                     RfVals V;
                     const int g = rf_group(P, q[lane], V);
-                    if (g >= 0) rf_slot_add(S, g, tid, V);
+                    if (g >= 0) rf_slot_add(S, g, tid, V, df);
                     __syncwarp();
                     if (lane < qn - 32) q[lane] = q[32 + lane];
                     __syncwarp();
@@ -222,7 +225,7 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         if (lane < qn) {
             RfVals V;
             const int g = rf_group(P, q[lane], V);
-            if (g >= 0) rf_slot_add(S, g, tid, V);
+            if (g >= 0) rf_slot_add(S, g, tid, V, df);
         }
         __syncwarp();
 #else
@@ -230,10 +233,11 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         for (long long r = r0 + tid; r < r1; r += T) {
             RfVals V;
             int g = rf_group(P, r, V);
-            if (g >= 0) rf_slot_add(S, g, tid, V);
+            if (g >= 0) rf_slot_add(S, g, tid, V, df);
         }
 #endif
     }
+    rf_slots_done(S, tid, df);
     __syncthreads();
     unsigned long long* part = (unsigned long long*)P.partials;
     for (int q = warp; q < Q; q += T / 32) {

@@ -1980,14 +1980,37 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
             o << "        case " << m << ": return " << enc(lf, e) << ";\n";
         }
         o << "        default: return a;\n    }\n}\n\n";
-        o << "RF_DEV void rf_slot_add(unsigned long long* S, int g, int t, const RfVals& V)\n{\n";
+        // FP64 SUM slots accumulate as double-floats on the FP32 pipe while `df` (the thread's
+        // mode for the unit) holds; an addend out of the double-float range turns every such slot
+        // of the thread into a double and the thread continues in FP64 (rf_df_slot_add in
+        // rf_device.cuh).  rf_slots_done leaves doubles in all slots for the block's fold.
+        std::vector<int> dfm;
         for (int m = 0; m < M; m++) {
-            o << "    { unsigned long long* s = S + (g * RF_M + " << m << ") * " << T << " + t; *s = rf_slot_combine("
-              << m << ", *s, ";
             auto& lf = leaves[g0[m]];
-            o << enc(lf, "V.v" + std::to_string(m)) << "); }\n";
+            if (lf.op == AggOp::SUM && !lf.count && lf.type.btype == FLOAT64) dfm.push_back(m);
+        }
+        o << "RF_DEV void rf_slots_done(unsigned long long* S, int t, bool& df)\n{\n";
+        if (!dfm.empty()) {
+            o << "    if (!df) return;\n    df = false;\n    for (int g = 0; g < RF_G; g++) {\n";
+            for (int m : dfm)
+                o << "        { unsigned long long* s = S + (g * RF_M + " << m << ") * " << T
+                  << " + t; *s = rf_df_slot_to_f64(*s); }\n";
+            o << "    }\n";
+        } else {
+            o << "    (void)S; (void)t; (void)df;\n";
         }
         o << "}\n\n";
+        o << "RF_DEV void rf_slot_add(unsigned long long* S, int g, int t, const RfVals& V, bool& df)\n{\n";
+        for (int m = 0; m < M; m++) {
+            auto& lf = leaves[g0[m]];
+            const bool is_df = std::find(dfm.begin(), dfm.end(), m) != dfm.end();
+            o << "    { unsigned long long* s = S + (g * RF_M + " << m << ") * " << T << " + t; ";
+            if (is_df) o << "if (!df || !rf_df_slot_add(s, V.v" << m << ")) { rf_slots_done(S, t, df); ";
+            o << "*s = rf_slot_combine(" << m << ", *s, " << enc(lf, "V.v" + std::to_string(m)) << ");";
+            if (is_df) o << " }";
+            o << " }\n";
+        }
+        o << "    (void)df;\n}\n\n";
 
         // group function
         Emitter E(*this);

@@ -193,3 +193,25 @@ def test_join_filtered_index_kept_between_runs(eng):
     assert again != first
     # back on the first table: its own answer, not the one the kept index would give
     assert plan.run(db, dp) == first
+
+
+def test_groupby_sums_of_one_sign_over_wide_magnitudes(eng):
+    # FP64 sums of positive addends spread over ~120 binades (each thread's sums kept as
+    # double-floats on the FP32 pipe while its addends stay in range and of one sign): within
+    # 1e-12 of the serial FP64 sums; sums of integers (the quantities) stay exact
+    t = W.groupby_table(700_001, seed=29)
+    rng = np.random.default_rng(29)
+    n = len(t)
+    price = t.columns[4].data
+    price[:] = rng.uniform(1.0, 2.0, n) * 2.0 ** rng.integers(-60, 60, n)
+    idx = rng.choice(n, 30, replace=False)
+    price[idx[:10]] = 2.0 ** 99       # the largest magnitude kept as a double-float
+    price[idx[10:20]] = 2.0 ** -103   # the smallest
+    price[idx[20:]] = 0.0
+    fn = W.groupby_query(t.get_data_type())
+    dt = eng.upload(t)
+    got = eng.compile(fn).run(dt)
+    ref = loopgen.Query(fn)(t)
+    assert_same(got, ref)
+    for g, r in zip(got, ref):
+        assert g[0] == r[0] and g[7] == r[7]  # SUM(quantity) of integers and COUNT: exact
