@@ -330,41 +330,36 @@ RF_DEV void rf_two_sum(float a, float b, float& s, float& e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-RF_DEV void rf_quick_two_sum(float a, float b, float& s, float& e)
+// (ah, al) += (bh, bl) for addends of the sum's sign: Knuth's two-sum of the high parts, the low
+// parts added to its error, one renormalisation (Dekker's fast two-sum).  Without cancellation
+// the pair stays within about 2^-47 of the exact sum, relative to the sum.
+RF_DEV void rf_df_add_same_sign(float& ah, float& al, float bh, float bl)
 {
-    s = __fadd_rn(a, b);
-    e = __fsub_rn(b, __fsub_rn(s, a));
+    float s, e;
+    rf_two_sum(ah, bh, s, e);
+    e = __fadd_rn(e, __fadd_rn(al, bl));
+    ah = __fadd_rn(s, e);
+    al = __fsub_rn(e, __fsub_rn(ah, s));
 }
 
-// (ah, al) += (bh, bl)
-RF_DEV void rf_df_add(float& ah, float& al, float bh, float bl)
-{
-    float s1, s2, t1, t2;
-    rf_two_sum(ah, bh, s1, s2);
-    rf_two_sum(al, bl, t1, t2);
-    s2 = __fadd_rn(s2, t1);
-    rf_quick_two_sum(s1, s2, s1, s2);
-    s2 = __fadd_rn(s2, t2);
-    rf_quick_two_sum(s1, s2, ah, al);
-}
-
-// a double-float slot += v.  False, with the slot unchanged, when v is out of the split's range,
-// when v and the sum so far have opposite signs, or when the sum would reach 2^120 (far below
-// the float range): the caller then turns its slots into doubles and adds v in FP64.  Addends of
-// one sign keep the sum well conditioned, so its relative error stays that of the additions
-// (about 2^-48 times the square root of their number, typically); a sum with cancellation is
-// left to FP64, whose error relative to the result is 32 times smaller.
-RF_DEV bool rf_df_slot_add(unsigned long long* s, double v)
+// one double-float slot update, in three steps the caller interleaves over a row's slots (so
+// their latencies overlap): split the addend, add it to the loaded pair, store.  rf_df_step
+// returns false, with nothing to store, when the addend is out of the split's range, has the
+// opposite sign of a non-zero sum, or the sum would reach 2^120 (far below the float range): the
+// caller then turns its slots into doubles and adds in FP64.  Addends of one sign keep the sum
+// well conditioned, so its relative error stays that of the additions (about 2^-48 times the
+// square root of their number, typically); a sum with cancellation is left to FP64, whose error
+// relative to the result is 32 times smaller.
+RF_DEV bool rf_df_step(unsigned long long w, double v, unsigned long long& out)
 {
     float bh, bl;
-    if (!rf_df_split(v, bh, bl)) return false;
-    const unsigned long long w = *s;
+    bool ok = rf_df_split(v, bh, bl);
     float ah = __uint_as_float((unsigned)w), al = __uint_as_float((unsigned)(w >> 32));
-    if (((unsigned)w ^ __float_as_uint(bh)) >> 31 && ah != 0.f && bh != 0.f) return false;
-    rf_df_add(ah, al, bh, bl);
-    if (!(fabsf(ah) < 0x1p120f)) return false;
-    *s = (unsigned long long)__float_as_uint(ah) | ((unsigned long long)__float_as_uint(al) << 32);
-    return true;
+    ok &= !(((unsigned)w ^ __float_as_uint(bh)) >> 31) || ah == 0.f || bh == 0.f;
+    rf_df_add_same_sign(ah, al, bh, bl);
+    ok &= fabsf(ah) < 0x1p120f;
+    out = (unsigned long long)__float_as_uint(ah) | ((unsigned long long)__float_as_uint(al) << 32);
+    return ok;
 }
 
 // the double nearest hi + lo of a double-float slot, as slot bits

@@ -284,12 +284,15 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
     __syncthreads();  // shared state is reused by the next work item of a persistent block
 }
 
+#ifndef RF_MINB
+#define RF_MINB 1
+#endif
 #define RF_GROUP_REDUCE_KERNEL(NAME, T)                                                     \
-    extern "C" __global__ void __launch_bounds__(T) NAME(const __grid_constant__ RfParams P) \
+    extern "C" __global__ void __launch_bounds__(T, RF_MINB) NAME(const __grid_constant__ RfParams P) \
     {                                                                                       \
         rf_group_reduce<T>(P, P.unit0 + (int)blockIdx.x, P.nunits);                         \
     }                                                                                       \
-    extern "C" __global__ void __launch_bounds__(T)                                         \
+    extern "C" __global__ void __launch_bounds__(T, RF_MINB)                                \
         rf_batch(const RfParams* __restrict__ params, const int2* __restrict__ work, const int* nwork) \
     {                                                                                       \
         const int n = *nwork;                                                               \

@@ -1981,36 +1981,59 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         }
         o << "        default: return a;\n    }\n}\n\n";
         // FP64 SUM slots accumulate as double-floats on the FP32 pipe while `df` (the thread's
-        // mode for the unit) holds; an addend out of the double-float range turns every such slot
-        // of the thread into a double and the thread continues in FP64 (rf_df_slot_add in
-        // rf_device.cuh).  rf_slots_done leaves doubles in all slots for the block's fold.
-        std::vector<int> dfm;
-        for (int m = 0; m < M; m++) {
-            auto& lf = leaves[g0[m]];
-            if (lf.op == AggOp::SUM && !lf.count && lf.type.btype == FLOAT64) dfm.push_back(m);
-        }
-        o << "RF_DEV void rf_slots_done(unsigned long long* S, int t, bool& df)\n{\n";
-        if (!dfm.empty()) {
-            o << "    if (!df) return;\n    df = false;\n    for (int g = 0; g < RF_G; g++) {\n";
-            for (int m : dfm)
-                o << "        { unsigned long long* s = S + (g * RF_M + " << m << ") * " << T
-                  << " + t; *s = rf_df_slot_to_f64(*s); }\n";
-            o << "    }\n";
-        } else {
-            o << "    (void)S; (void)t; (void)df;\n";
-        }
-        o << "}\n\n";
-        o << "RF_DEV void rf_slot_add(unsigned long long* S, int g, int t, const RfVals& V, bool& df)\n{\n";
-        for (int m = 0; m < M; m++) {
-            auto& lf = leaves[g0[m]];
-            const bool is_df = std::find(dfm.begin(), dfm.end(), m) != dfm.end();
-            o << "    { unsigned long long* s = S + (g * RF_M + " << m << ") * " << T << " + t; ";
-            if (is_df) o << "if (!df || !rf_df_slot_add(s, V.v" << m << ")) { rf_slots_done(S, t, df); ";
-            o << "*s = rf_slot_combine(" << m << ", *s, " << enc(lf, "V.v" + std::to_string(m)) << ");";
-            if (is_df) o << " }";
-            o << " }\n";
-        }
-        o << "    (void)df;\n}\n\n";
+        // mode for the unit) holds, in kernels whose rows mostly reach the slots (not in a
+        // compacting probe kernel: there few rows add anything, and the longer slot update costs
+        // the probes occupancy - the 200M-row join measured 1.11 -> 1.23 ms with it)
+        auto emit_slot_add = [&](std::ostream& so, bool use_df) {
+            // an addend out of the double-float range turns every such slot of the thread into a
+            // double and the thread continues in FP64 (rf_df_step in rf_device.cuh); rf_slots_done
+            // leaves doubles in all slots for the block's fold
+            std::vector<int> dfm;
+            for (int m = 0; m < M; m++) {
+                auto& lf = leaves[g0[m]];
+                if (use_df && lf.op == AggOp::SUM && !lf.count && lf.type.btype == FLOAT64) dfm.push_back(m);
+            }
+            so << "RF_DEV void rf_slots_done(unsigned long long* S, int t, bool& df)\n{\n";
+            if (!dfm.empty()) {
+                so << "    if (!df) return;\n    df = false;\n    for (int g = 0; g < RF_G; g++) {\n";
+                for (int m : dfm)
+                    so << "        { unsigned long long* s = S + (g * RF_M + " << m << ") * " << T
+                      << " + t; *s = rf_df_slot_to_f64(*s); }\n";
+                so << "    }\n";
+            } else {
+                so << "    (void)S; (void)t; (void)df;\n";
+            }
+            so << "}\n\n";
+            so << "RF_DEV void rf_slot_add(unsigned long long* S, int g, int t, const RfVals& V, bool& df)\n{\n";
+            auto slot_ptr = [&](int m) {
+                return "S + (g * RF_M + " + std::to_string(m) + ") * " + std::to_string(T) + " + t";
+            };
+            if (!dfm.empty()) {
+                // every double-float slot of the row in one pass (independent latency chains), one
+                // combined check, then all stores - or the switch to FP64 for the rest of the unit
+                so << "    bool fp64 = !df;\n    if (df) {\n        bool ok = true;\n";
+                for (int m : dfm)
+                    so << "        unsigned long long* p" << m << " = " << slot_ptr(m) << ", n" << m << ";\n";
+                for (int m : dfm) so << "        ok &= rf_df_step(*p" << m << ", V.v" << m << ", n" << m << ");\n";
+                so << "        if (ok) {\n";
+                for (int m : dfm) so << "            *p" << m << " = n" << m << ";\n";
+                so << "        } else {\n            rf_slots_done(S, t, df);\n            fp64 = true;\n        }\n    }\n";
+                so << "    if (fp64) {\n";
+                for (int m : dfm) {
+                    auto& lf = leaves[g0[m]];
+                    so << "        { unsigned long long* s = " << slot_ptr(m) << "; *s = rf_slot_combine(" << m << ", *s, "
+                      << enc(lf, "V.v" + std::to_string(m)) << "); }\n";
+                }
+                so << "    }\n";
+            }
+            for (int m = 0; m < M; m++) {
+                if (std::find(dfm.begin(), dfm.end(), m) != dfm.end()) continue;
+                auto& lf = leaves[g0[m]];
+                so << "    { unsigned long long* s = " << slot_ptr(m) << "; *s = rf_slot_combine(" << m << ", *s, "
+                  << enc(lf, "V.v" + std::to_string(m)) << "); }\n";
+            }
+            so << "    (void)df;\n}\n\n";
+        };
 
         // group function
         Emitter E(*this);
@@ -2106,6 +2129,7 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
             }
         }
 
+        emit_slot_add(o, !compact);
         push_index_filter(o, red, filters);
         // A grouped scan that reads every row's columns prefetches the next tile into L2 while it
         // works on this one (the 60M-row, 6-group group-by: 1.23 -> 1.15 ms; its FP64 work waited
@@ -2141,10 +2165,17 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         o << fb.str() << stores.str() << "}\n\n";
 
         src << o.str();
-        src << "#define RF_GROUP_REDUCE 1\n#include \"rf_templates.cuh\"\n";
-        src << "RF_GROUP_REDUCE_KERNEL(rf_main, " << T << ")\n";
         size_t smem = (size_t)G * M * T * 8 + (compact ? (size_t)(T / 32) * 64 * 8 : 0);
         if (smem > 200 * 1024) throw LowerError("too many group accumulators for shared memory");
+        // the blocks an SM holds by shared memory (228 KiB, 1 KiB reserved per block) are the
+        // blocks the registers should allow too, so the compiler is asked to fit that many - down
+        // to 80 registers a thread (the double-float slot update of the 6-group group-by needs
+        // about that many; a compacting probe kernel keeps the compiler's own choice)
+        const int minb = compact ? 1
+                                 : (int)std::max<size_t>(1, std::min<size_t>({(size_t)2048 / T, (228 * 1024) / (smem + 1024),
+                                                                              (size_t)65536 / (80 * (size_t)T)}));
+        src << "#define RF_GROUP_REDUCE 1\n#define RF_MINB " << minb << "\n#include \"rf_templates.cuh\"\n";
+        src << "RF_GROUP_REDUCE_KERNEL(rf_main, " << T << ")\n";
         plan_.kernels.push_back({"rf_main", T, smem, KernelSpec::MAIN});
         plan_.acc_bytes = (size_t)G * M * 8;
     }
