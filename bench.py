@@ -846,7 +846,8 @@ def main():
                 "tuning": dict(head["tuning"] or {}, source="autotuner (rf_plan_tune) before warm-up"),
                 "bytes_per_step": head["bytes_per_step"], "rows_per_s": head["rows_per_s"],
                 "roofline": head["roofline"], "cpu_baseline": head["cpu_baseline"], "e2e": head["e2e"],
-                "parity": head["parity"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
+                "parity": head["parity"], "parity_reffine_code": head.get("parity_reffine_code"),
+                "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
                 "per_config": per_config or None, "serving": serving, "result_sample": head["result_sample"]}
         if "bytes_mismatch" in head:
             line["bytes_mismatch"] = head["bytes_mismatch"]
