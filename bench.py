@@ -783,6 +783,9 @@ def main():
                     help="write the autotuner's choices to this JSON file after tuning")
     ap.add_argument("--tune-file", default="",
                     help="take the autotuner's choices from this JSON file instead of tuning (profiling runs)")
+    ap.add_argument("--tune-as-rows", type=int, default=0,
+                    help="with --tune-file: apply the file's tilings to tables of this many rows too (a "
+                         "smaller profiling case run with the full-size configuration)")
     ap.add_argument("--ingest", action="store_true",
                     help="measure Arrow IPC ingest of the config's table instead (one JSON line)")
     ap.add_argument("--serving-only", action="store_true",
@@ -811,7 +814,18 @@ def main():
     dist = Dist(world)
     eng = engine.Engine(local)
     if args.tune_file:
-        eng.tune_load(args.tune_file)  # compiles below take the file's block sizes and tilings
+        path = args.tune_file
+        if args.tune_as_rows > 0:
+            # each tiling entry (bucket >= 0: the size class floor(log2(rows))) copied to the
+            # bucket of the given row count; the block sizes (bucket -1) hold for every size
+            with open(path) as f:
+                tune = json.load(f)
+            b = max(0, args.tune_as_rows.bit_length() - 1)
+            tune["entries"] += [dict(e, bucket=b) for e in tune["entries"] if e["bucket"] >= 0]
+            path = path + ".as%d.json" % args.tune_as_rows
+            with open(path, "w") as f:
+                json.dump(tune, f)
+        eng.tune_load(path)  # compiles below take the file's block sizes and tilings
     wl = build_workload(args.config, rank, world, args.rows)
     head = measure_config(eng, wl, args.config, args, rank, world, dist, cpu=not args.no_cpu)
     del wl
