@@ -284,15 +284,20 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
     __syncthreads();  // shared state is reused by the next work item of a persistent block
 }
 
-#ifndef RF_MINB
-#define RF_MINB 1
+// RF_MINB (set by the fragment): the blocks per SM the registers must allow; unset, the bound
+// names the block size alone (a minimum of 1 block measured slower for the join's probe kernel:
+// 1.11 -> 1.39 ms, as the compiler then takes registers freely)
+#ifdef RF_MINB
+#define RF_GROUP_BOUNDS(T) __launch_bounds__(T, RF_MINB)
+#else
+#define RF_GROUP_BOUNDS(T) __launch_bounds__(T)
 #endif
 #define RF_GROUP_REDUCE_KERNEL(NAME, T)                                                     \
-    extern "C" __global__ void __launch_bounds__(T, RF_MINB) NAME(const __grid_constant__ RfParams P) \
+    extern "C" __global__ void RF_GROUP_BOUNDS(T) NAME(const __grid_constant__ RfParams P) \
     {                                                                                       \
         rf_group_reduce<T>(P, P.unit0 + (int)blockIdx.x, P.nunits);                         \
     }                                                                                       \
-    extern "C" __global__ void __launch_bounds__(T, RF_MINB)                                \
+    extern "C" __global__ void RF_GROUP_BOUNDS(T)                                           \
         rf_batch(const RfParams* __restrict__ params, const int2* __restrict__ work, const int* nwork) \
     {                                                                                       \
         const int n = *nwork;                                                               \

@@ -2174,7 +2174,9 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         const int minb = compact ? 1
                                  : (int)std::max<size_t>(1, std::min<size_t>({(size_t)2048 / T, (228 * 1024) / (smem + 1024),
                                                                               (size_t)65536 / (80 * (size_t)T)}));
-        src << "#define RF_GROUP_REDUCE 1\n#define RF_MINB " << minb << "\n#include \"rf_templates.cuh\"\n";
+        src << "#define RF_GROUP_REDUCE 1\n";
+        if (minb > 1) src << "#define RF_MINB " << minb << "\n";
+        src << "#include \"rf_templates.cuh\"\n";
         src << "RF_GROUP_REDUCE_KERNEL(rf_main, " << T << ")\n";
         plan_.kernels.push_back({"rf_main", T, smem, KernelSpec::MAIN});
         plan_.acc_bytes = (size_t)G * M * 8;
