@@ -1586,7 +1586,10 @@ private:
         std::vector<std::string> dcls(E.decls.begin(), E.decls.end());
         std::vector<std::string*> pieces{&rowcond, &updates};
         for (auto& d : dcls) pieces.push_back(&d);
-        std::string condtext = rowcond + allconds;
+        // a scan's row reads every column it references up front, the columns its values read
+        // too (not after the filter passes: a load issued only then is a second round trip to
+        // memory per row, and the 4-row vector loads fetch whole sectors anyway)
+        std::string condtext = rowcond + allconds + updates;
         std::string hoisted = hoist_row_loads(condtext, pieces);
         // the hoisted loads ("    const T ldK = rf_ld<T>(COL.data, r);") become parameters of the
         // row body rf_row_v, so that rf_row (one row) and rf_row4 (4 rows from vector loads) share it
