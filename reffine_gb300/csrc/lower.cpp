@@ -2564,6 +2564,10 @@ extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_con
     unsigned long long* tab = (unsigned long long*)P.aux4;
     unsigned long long* wa = wacc + (size_t)warp * RF_HG_HK * RF_HG_L;
     unsigned long long* x = xs + ((size_t)warp * 32 + lane) * RF_HG_L;
+    unsigned long long top[RF_HG_L];  // the lane's sums of hot id 0
+#pragma unroll
+    for (int l = 0; l < RF_HG_L; l++) top[l] = rf_hg_identity(P, l);
+    bool top_seen = false;
     const long long n = P.aux_n0;
     const unsigned long long C = (unsigned long long)P.aux_n1;
     // whole warps step together (the fold needs every lane); rows past the end are inactive.  A
@@ -2603,9 +2607,26 @@ extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_con
         }
 #pragma unroll
         for (int j = 0; j < RF_HG_U; j++) {
-            // fold of the hottest keys: lanes of one hot key find each other, the lowest folds
-            const unsigned peers = __match_any_sync(0xffffffffu, h[j] >= 0 ? h[j] : -1 - lane);
-            if (h[j] >= 0) {
+            // the hottest key (hot id 0, about a tenth of the rows under Zipf(1.1)) adds into the
+            // lane's own registers: no fold, and the other hot keys' folds stay short
+            if (h[j] == 0) {
+                unsigned long long xr[RF_HG_L];
+                rf_hg_vals(P, row[j], xr);
+#pragma unroll
+                for (int l = 0; l < RF_HG_L; l++) top[l] = rf_hg_comb(l, top[l], xr[l]);
+                top_seen = true;
+            }
+            // fold of the other hottest keys: lanes of one hot key find each other, the lowest
+            // folds; a key alone in the warp adds straight into the warp's accumulators
+            const unsigned peers = __match_any_sync(0xffffffffu, h[j] >= 1 ? h[j] : -1 - lane);
+            if (h[j] >= 1 && peers == (1u << lane)) {
+                unsigned long long xr[RF_HG_L];
+                rf_hg_vals(P, row[j], xr);
+                unsigned long long* A = wa + (size_t)h[j] * RF_HG_L;
+#pragma unroll
+                for (int l = 0; l < RF_HG_L; l++) A[l] = rf_hg_comb(l, A[l], xr[l]);
+                seen[h[j]] = 1;
+            } else if (h[j] >= 1) {
                 rf_hg_vals(P, row[j], x);
                 __syncwarp(peers);
                 if (lane == __ffs(peers) - 1) {
@@ -2645,6 +2666,17 @@ extern "C" __global__ void __launch_bounds__(RF_HG_T) rf_hg_agg(const __grid_con
             }
             if (g >= 0) rf_hg_apply(P, row[j], tab + g * RF_HG_SW + 1, 1);
         }
+    }
+    // the lanes' sums of hot id 0 into their warp's accumulator of it
+    if (__any_sync(0xffffffffu, top_seen)) {
+#pragma unroll
+        for (int l = 0; l < RF_HG_L; l++) {
+            unsigned long long v = top[l];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v = rf_hg_comb(l, v, __shfl_down_sync(0xffffffffu, v, off));
+            if (lane == 0) wa[l] = rf_hg_comb(l, wa[l], v);
+        }
+        if (lane == 0) seen[0] = 1;
     }
     __syncthreads();
     // warp accumulators of each hottest key, folded over the warps, then into the global table
