@@ -291,34 +291,34 @@ RF_DEV double rf_u2f(unsigned long long x) { return __longlong_as_double((long l
 // ---------------------------------------------------------------------------------------
 // FP64 sums on the FP32 pipe.  GB300's FP64 pipe issues about 1/64 of its FP32 rate, and a
 // grouped scan spends most of it on its sums.  A sum slot can instead hold an unevaluated pair of
-// floats hi + lo (a "double-float", 48 significant bits): each addend is split into two floats
-// with integer operations only, and added with the error-free two-sum of Knuth (TAOCP vol. 2,
-// 4.2.2) and Dekker's renormalisation (the accurate double-float addition of Hida, Li and Bailey's
-// QD library): the pair stays within about 2^-47 of the exact running sum, relative to the sum.
+// floats hi + lo (a "double-float", 48 significant bits) while its addends are non-negative: each
+// addend is split into two floats with integer operations only, and added with the error-free
+// two-sum of Knuth (TAOCP vol. 2, 4.2.2) and Dekker's renormalisation (as in the double-float
+// additions of Hida, Li and Bailey's QD library): the pair stays within about 2^-47 of the exact
+// running sum, relative to the sum.
 // FP64 sums of the same rows in another order differ by the same order of rounding, far inside
 // the 1e-12 relative tolerance kept against the serial reference loop.
 // A slot's 64 bits hold the pair (hi in the low word, lo in the high word); +0.0 is all zeros in
 // both encodings.
 // ---------------------------------------------------------------------------------------
 
-// v = hi + lo, |hi + lo - v| <= 2^-47 |v|; false (and nothing set) unless v is +-0 or a normal
-// double of magnitude in [2^-103, 2^100): subnormals, larger values, infinities and NaN are left
-// to FP64 arithmetic.  hi takes the sign, the exponent and the leading 23 fraction bits of v (so
-// hi is v truncated to 24 bits); lo the next 23, rounded to nearest on the 6 bits after them,
-// built as (1.m - 1.0) x 2^k from two floats with the same exponent, which subtract exactly.
+// v = hi + lo for a non-negative v, |hi + lo - v| <= 2^-47 v; false (and nothing set) unless v is
+// +0 or a normal double in [2^-103, 2^91): negative values, -0, subnormals, larger values,
+// infinities and NaN are left to FP64 arithmetic.  hi takes the exponent and the leading 23
+// fraction bits of v (so hi is v truncated to 24 bits); lo the next 23, rounded to nearest on the
+// 6 bits after them, built as (1.m - 1.0) x 2^k from two floats with the same exponent, which
+// subtract exactly.  One unsigned compare on the high word tests sign and exponent together.
 RF_DEV bool rf_df_split(double v, float& hi, float& lo)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
     const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
-    const unsigned e = (h >> 20) & 0x7FFu;
-    if (e - 920u >= 204u) {
+    if (h - (920u << 20) >= (194u << 20)) {
         hi = 0.f;
         lo = 0.f;
-        return (b << 1) == 0ULL;
+        return b == 0ULL;
     }
-    const unsigned s = h & 0x80000000u;
-    hi = __uint_as_float(s | ((h - (896u << 20)) << 3) | (l >> 29));
-    const unsigned c = s | ((e - 919u) << 23);
+    hi = __uint_as_float(((h - (896u << 20)) << 3) | (l >> 29));
+    const unsigned c = ((h - (919u << 20)) >> 20) << 23;
     lo = __uint_as_float(c + (((l & 0x1FFFFFFFu) + 32u) >> 6)) - __uint_as_float(c);
     return true;
 }
@@ -330,9 +330,9 @@ RF_DEV void rf_two_sum(float a, float b, float& s, float& e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// (ah, al) += (bh, bl) for addends of the sum's sign: Knuth's two-sum of the high parts, the low
-// parts added to its error, one renormalisation (Dekker's fast two-sum).  Without cancellation
-// the pair stays within about 2^-47 of the exact sum, relative to the sum.
+// (ah, al) += (bh, bl) for non-negative pairs: Knuth's two-sum of the high parts, the low parts
+// added to its error, one renormalisation (Dekker's fast two-sum).  Without cancellation the
+// pair stays within about 2^-47 of the exact sum, relative to the sum.
 RF_DEV void rf_df_add_same_sign(float& ah, float& al, float bh, float bl)
 {
     float s, e;
@@ -344,20 +344,20 @@ RF_DEV void rf_df_add_same_sign(float& ah, float& al, float bh, float bl)
 
 // one double-float slot update, in three steps the caller interleaves over a row's slots (so
 // their latencies overlap): split the addend, add it to the loaded pair, store.  rf_df_step
-// returns false, with nothing to store, when the addend is out of the split's range, has the
-// opposite sign of a non-zero sum, or the sum would reach 2^120 (far below the float range): the
-// caller then turns its slots into doubles and adds in FP64.  Addends of one sign keep the sum
-// well conditioned, so its relative error stays that of the additions (about 2^-48 times the
-// square root of their number, typically); a sum with cancellation is left to FP64, whose error
-// relative to the result is 32 times smaller.
+// returns false, with nothing to store, when the addend is not a non-negative value in the
+// split's range: the caller then turns its slots into doubles and adds in FP64.  A slot so only
+// ever sums non-negative values, which keeps the sum well conditioned: its relative error stays
+// that of the additions (about 2^-48 times the square root of their number, typically), and it
+// cannot reach the float range (addends below 2^91; a thread adds fewer than 2^36 of them to a
+// slot in one work unit, far more rows than device memory holds).  Sums with negative addends,
+// where cancellation can occur, are left to FP64, whose error relative to the result is 32 times
+// smaller.
 RF_DEV bool rf_df_step(unsigned long long w, double v, unsigned long long& out)
 {
     float bh, bl;
-    bool ok = rf_df_split(v, bh, bl);
+    const bool ok = rf_df_split(v, bh, bl);
     float ah = __uint_as_float((unsigned)w), al = __uint_as_float((unsigned)(w >> 32));
-    ok &= !(((unsigned)w ^ __float_as_uint(bh)) >> 31) || ah == 0.f || bh == 0.f;
     rf_df_add_same_sign(ah, al, bh, bl);
-    ok &= fabsf(ah) < 0x1p120f;
     out = (unsigned long long)__float_as_uint(ah) | ((unsigned long long)__float_as_uint(al) << 32);
     return ok;
 }

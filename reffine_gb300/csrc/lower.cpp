@@ -1988,9 +1988,9 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         // compacting probe kernel: there few rows add anything, and the longer slot update costs
         // the probes occupancy - the 200M-row join measured 1.11 -> 1.23 ms with it)
         auto emit_slot_add = [&](std::ostream& so, bool use_df) {
-            // an addend out of the double-float range turns every such slot of the thread into a
-            // double and the thread continues in FP64 (rf_df_step in rf_device.cuh); rf_slots_done
-            // leaves doubles in all slots for the block's fold
+            // an addend that is negative or out of the double-float range turns every such slot of
+            // the thread into a double and the thread continues in FP64 (rf_df_step in
+            // rf_device.cuh); rf_slots_done leaves doubles in all slots for the block's fold
             std::vector<int> dfm;
             for (int m = 0; m < M; m++) {
                 auto& lf = leaves[g0[m]];

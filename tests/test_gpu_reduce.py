@@ -197,16 +197,18 @@ def test_join_filtered_index_kept_between_runs(eng):
 
 def test_groupby_sums_of_one_sign_over_wide_magnitudes(eng):
     # FP64 sums of positive addends spread over ~120 binades (each thread's sums kept as
-    # double-floats on the FP32 pipe while its addends stay in range and of one sign): within
-    # 1e-12 of the serial FP64 sums; sums of integers (the quantities) stay exact
+    # double-floats on the FP32 pipe while its addends stay non-negative and in range, FP64 after
+    # the first that is not): within 1e-12 of the serial FP64 sums; sums of integers (the
+    # quantities) stay exact
     t = W.groupby_table(700_001, seed=29)
     rng = np.random.default_rng(29)
     n = len(t)
     price = t.columns[4].data
     price[:] = rng.uniform(1.0, 2.0, n) * 2.0 ** rng.integers(-60, 60, n)
     idx = rng.choice(n, 30, replace=False)
-    price[idx[:10]] = 2.0 ** 99       # the largest magnitude kept as a double-float
-    price[idx[10:20]] = 2.0 ** -103   # the smallest
+    price[idx[:5]] = 2.0 ** 90        # kept as a double-float
+    price[idx[5:10]] = 2.0 ** 99      # beyond the double-float range: that thread continues in FP64
+    price[idx[10:20]] = 2.0 ** -103   # the smallest kept
     price[idx[20:]] = 0.0
     fn = W.groupby_query(t.get_data_type())
     dt = eng.upload(t)
