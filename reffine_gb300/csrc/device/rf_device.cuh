@@ -310,17 +310,15 @@ RF_DEV double rf_u2f(unsigned long long x) { return __longlong_as_double((long l
 // subtract exactly.  One unsigned compare on the high word tests sign and exponent together.
 RF_DEV bool rf_df_split(double v, float& hi, float& lo)
 {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
-    if (h - (920u << 20) >= (194u << 20)) {
-        hi = 0.f;
-        lo = 0.f;
-        return b == 0ULL;
-    }
-    hi = __uint_as_float(((h - (896u << 20)) << 3) | (l >> 29));
-    const unsigned c = ((h - (919u << 20)) >> 20) << 23;
-    lo = __uint_as_float(c + (((l & 0x1FFFFFFFu) + 32u) >> 6)) - __uint_as_float(c);
-    return true;
+    const unsigned h = (unsigned)__double2hiint(v), l = (unsigned)__double2loint(v);
+    // computed whatever the range (no branch), kept only in range
+    const bool in = h - (920u << 20) < (194u << 20);
+    const unsigned hb = __funnelshift_l(l, h - (896u << 20), 3);  // exponent - 896, 23 fraction bits
+    const unsigned c = (hb & 0x7F800000u) - (23u << 23);           // 2^(exponent of v - 23)
+    const float lf = __uint_as_float(c + (((l & 0x1FFFFFFFu) + 32u) >> 6)) - __uint_as_float(c);
+    hi = in ? __uint_as_float(hb) : 0.f;
+    lo = in ? lf : 0.f;
+    return in || (h | l) == 0u;
 }
 
 RF_DEV void rf_two_sum(float a, float b, float& s, float& e)
@@ -352,13 +350,12 @@ RF_DEV void rf_df_add_same_sign(float& ah, float& al, float bh, float bl)
 // slot in one work unit, far more rows than device memory holds).  Sums with negative addends,
 // where cancellation can occur, are left to FP64, whose error relative to the result is 32 times
 // smaller.
-RF_DEV bool rf_df_step(unsigned long long w, double v, unsigned long long& out)
+RF_DEV bool rf_df_step(float2 a, double v, float2& out)
 {
     float bh, bl;
     const bool ok = rf_df_split(v, bh, bl);
-    float ah = __uint_as_float((unsigned)w), al = __uint_as_float((unsigned)(w >> 32));
-    rf_df_add_same_sign(ah, al, bh, bl);
-    out = (unsigned long long)__float_as_uint(ah) | ((unsigned long long)__float_as_uint(al) << 32);
+    rf_df_add_same_sign(a.x, a.y, bh, bl);
+    out = a;
     return ok;
 }
 

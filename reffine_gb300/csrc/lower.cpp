@@ -2016,7 +2016,7 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
                 // combined check, then all stores - or the switch to FP64 for the rest of the unit
                 so << "    bool fp64 = !df;\n    if (df) {\n        bool ok = true;\n";
                 for (int m : dfm)
-                    so << "        unsigned long long* p" << m << " = " << slot_ptr(m) << ", n" << m << ";\n";
+                    so << "        float2* p" << m << " = (float2*)(" << slot_ptr(m) << ");\n        float2 n" << m << ";\n";
                 for (int m : dfm) so << "        ok &= rf_df_step(*p" << m << ", V.v" << m << ", n" << m << ");\n";
                 so << "        if (ok) {\n";
                 for (int m : dfm) so << "            *p" << m << " = n" << m << ";\n";
