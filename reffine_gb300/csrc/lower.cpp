@@ -2056,15 +2056,17 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
             gconds += kc;
             gb << "    const auto key" << k << " = " << kc << ";\n";
         }
+        // the group whose keys match, as selects from the last group to the first (the first
+        // match wins, as in an if-else chain, without a branch per group)
         gb << "    int g = -1;\n";
-        for (int g = 0; g < G; g++) {
+        for (int g = G - 1; g >= 0; g--) {
             auto& lf = leaves[groups[g][0]];
-            gb << "    " << (g ? "else if (" : "if (");
+            gb << "    g = (";
             for (size_t k = 0; k < key_exprs.size(); k++) {
                 if (k) gb << " && ";
                 gb << "(key" << k << " == " << E.ev(lf.keys[k].second).c << ")";
             }
-            gb << ") g = " << g << ";\n";
+            gb << ") ? " << g << " : g;\n";
         }
         gb << "    if (g < 0) return -1;\n";
         for (int m = 0; m < M; m++) {
