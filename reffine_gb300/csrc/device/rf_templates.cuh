@@ -229,7 +229,14 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         }
         __syncwarp();
 #else
+        // RF_GROUP_UNROLL 1 (a fragment with double-float sums): one row per iteration - the slot
+        // update is long, and unrolled rows cost registers the row's own latencies need (the
+        // 6-group group-by: 0.775 ms against 0.789 / 0.800 ms unrolled 2 / 4)
+#if defined(RF_GROUP_UNROLL) && RF_GROUP_UNROLL == 1
+#pragma unroll 1
+#else
 #pragma unroll 4
+#endif
         for (long long r = r0 + tid; r < r1; r += T) {
             RfVals V;
             int g = rf_group(P, r, V);

@@ -1996,6 +1996,7 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
                 auto& lf = leaves[g0[m]];
                 if (use_df && lf.op == AggOp::SUM && !lf.count && lf.type.btype == FLOAT64) dfm.push_back(m);
             }
+            if (!dfm.empty()) so << "#define RF_GROUP_UNROLL 1\n\n";
             so << "RF_DEV void rf_slots_done(unsigned long long* S, int t, bool& df)\n{\n";
             if (!dfm.empty()) {
                 so << "    if (!df) return;\n    df = false;\n    for (int g = 0; g < RF_G; g++) {\n";
