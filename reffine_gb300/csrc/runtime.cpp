@@ -1767,17 +1767,26 @@ int tune_tiles(rf_plan* p, const rf_arg* args, int32_t n_args, int32_t reps, int
         const long long t = ((rows + units - 1) / units + 3) & ~3LL;
         if (t >= 256 && t <= 65536 && std::find(cand.begin(), cand.end(), t) == cand.end()) cand.push_back(t);
     }
+    // each timing runs k launches back to back (k such that they take about 2 ms: a short kernel
+    // timed alone is mostly launch latency and its jitter), as a query stream runs them; the
+    // median of `reps` timings, after one warm-up launch
+    int k = 1;
     for (long long t : cand) {
         p->tile_override = t;
         std::vector<float> v;
         for (int r = 0; r <= reps && !rc; r++) {
+            const int n = r ? k : 1;
             cudaEventRecord(e0, s);
-            rc = enqueue(p, args, n_args, s, nullptr);
+            for (int i = 0; i < n && !rc; i++) rc = enqueue(p, args, n_args, s, nullptr);
             cudaEventRecord(e1, s);
             if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(ctx, RF_ERR_CUDA, "autotuner timing");
             float x = 0;
             cudaEventElapsedTime(&x, e0, e1);
-            if (r) v.push_back(x);  // the first run is a warm-up
+            if (!r) {
+                if (t == cand.front()) k = (int)std::max(1.0, std::min(64.0, std::ceil(2.0 / std::max(x, 1e-3f))));
+                continue;  // the first run is a warm-up
+            }
+            v.push_back(x / (float)n);
         }
         if (rc) break;
         std::sort(v.begin(), v.end());
