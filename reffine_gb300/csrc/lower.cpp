@@ -2083,8 +2083,14 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         std::vector<std::string> dcls(E.decls.begin(), E.decls.end());
         std::vector<std::string*> pieces{&rowcond, &gbody};
         for (auto& dd : dcls) pieces.push_back(&dd);
-        std::string hoisted = hoist_row_loads(rowcond + gconds, pieces);
-        {
+        // Without an index probe every column of the row is read up front, the value columns
+        // with the filter's and the keys' (one round trip to memory per row, not a second one
+        // once the row has passed).  A row that reaches a probe loads its values after it, so
+        // that rows failing the probe do not pay for them.
+        bool probes = gbody.find("rf_locate") != std::string::npos || rowcond.find("rf_locate") != std::string::npos;
+        for (auto& dd : dcls) probes = probes || dd.find("rf_locate") != std::string::npos;
+        std::string hoisted = hoist_row_loads(rowcond + gconds + (probes ? std::string() : gbody), pieces);
+        if (probes) {
             const std::string mk = "    if (g < 0) return -1;\n";
             const size_t at = gbody.find(mk);
             if (at != std::string::npos) hoist_value_loads(gbody, at + mk.size());
