@@ -598,7 +598,23 @@ private:
             switch (n.op) {
                 case MathOp::ADD: return scalar("(" + a(0) + " + " + a(1) + ")", n.type);
                 case MathOp::SUB: return scalar("(" + a(0) + " - " + a(1) + ")", n.type);
-                case MathOp::MUL: return scalar("(" + a(0) + " * " + a(1) + ")", n.type);
+                case MathOp::MUL:
+                    // x * (1 - y) and x * (1 + y) in binary64 as one fused multiply-add
+                    // (rf_mul_1m / rf_mul_1p in rf_device.cuh: one FP64 operation instead of two)
+                    if (n.type.btype == FLOAT64)
+                        for (size_t s = 0; s < 2; s++) {
+                            const Expr& f = n.args[1 - s];
+                            const bool sub = is_nary(f, MathOp::SUB), add = is_nary(f, MathOp::ADD);
+                            if (!sub && !add) continue;
+                            auto fn = as<NaryExpr>(f);
+                            if (!is_kind(fn->args[0], NodeKind::CONST) || fn->args[0]->type.btype != FLOAT64 ||
+                                fn->args[1]->type.btype != FLOAT64 || as<Const>(fn->args[0])->val != 1.0)
+                                continue;
+                            return scalar(std::string(sub ? "rf_mul_1m(" : "rf_mul_1p(") + a(s) + ", " +
+                                              ev(fn->args[1]).c + ")",
+                                          n.type);
+                        }
+                    return scalar("(" + a(0) + " * " + a(1) + ")", n.type);
                 case MathOp::DIV: return scalar("(" + a(0) + " / " + a(1) + ")", n.type);
                 case MathOp::MOD: return scalar("(" + a(0) + " % " + a(1) + ")", n.type);
                 case MathOp::MAX: return scalar("rf_max<" + T + ">(" + a(0) + ", " + a(1) + ")", n.type);

@@ -151,6 +151,34 @@ def test_groupby_fused_products_nonfinite(eng):
     assert_same(got, loopgen.Query(fn)(t))
 
 
+def test_groupby_fused_products_band_edges(eng):
+    # x*(1-y) and x*(1+y) are one fused multiply-add only for |x| in [2^-500, 2^500) and
+    # |y| < 2^500; rows at and beyond those edges, near overflow, subnormal, and with 1 -/+ y
+    # cancelling, must agree with the twice-rounded products
+    t = W.groupby_table(300_007, seed=29)
+    price, disc, tax = (t.columns[i].data for i in (4, 5, 6))
+    rng = np.random.default_rng(29)
+    idx = rng.choice(len(t), 16, replace=False)
+    price[idx[0]] = 2.0 ** 500               # first value above the band
+    price[idx[1]] = np.nextafter(2.0 ** 500, 0)
+    price[idx[2]] = 2.0 ** -500              # lowest value in the band
+    price[idx[3]] = np.nextafter(2.0 ** -500, 0)
+    price[idx[4]] = 1.0e308
+    disc[idx[4]] = -0.9                      # 1.9e308: overflows in both forms
+    price[idx[5]] = 5e-324                   # subnormal
+    disc[idx[6]] = 2.0 ** 500
+    tax[idx[7]] = 2.0 ** 600
+    disc[idx[8]] = 1.0 - 2.0 ** -52          # 1 - y exact and tiny
+    disc[idx[9]] = 1.0 + 2.0 ** -52          # a negative product
+    tax[idx[10]] = -1.0 + 2.0 ** -52         # 1 + y exact and tiny
+    tax[idx[11]] = -1.0                      # 1 + y = 0
+    price[idx[12]] = -3.5                    # a negative product, -0 from 1 - y = 0
+    disc[idx[12]] = 1.0
+    fn = W.groupby_query(t.get_data_type())
+    got = eng.compile(fn).run(eng.upload(t))
+    assert_same(got, loopgen.Query(fn)(t))
+
+
 def test_groupby_mixed_signs_wide_exponents(eng):
     # grouped FP64 sums over addends of both signs spread over ~60 binades, with tiny, huge,
     # subnormal and signed-zero values at random rows
