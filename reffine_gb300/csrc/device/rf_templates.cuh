@@ -153,7 +153,8 @@ RF_DEV void rf_scan_reduce_merge(const RfParams& P, int unit, int nunits, RfAcc&
 //   (group id or -1, and the row's aggregate inputs), rf_slot_init(m) (64-bit identity),
 //   rf_slot_combine(m, a, b), rf_slot_add(S, g, t, V, df), rf_slots_done(S, t, df) (df: the
 //   thread keeps its FP64 sums as double-floats, see rf_device.cuh) and
-//   rf_finish_groups(P, tot, out).
+//   rf_finish_groups(P, tot, out).  With RF_GROUP_SPLIT it also defines the row's loads apart,
+//   struct RfRowLd, rf_group_ld(P, r, L) and rf_group_v(P, r, L, V) (rf_group is the two in turn).
 // Each thread owns a private column of G*M 64-bit slots in shared memory (slot (q, t) at
 // S[q * T + t]): no atomics and no bank conflicts on the per-row update.  At the end every
 // slot column is folded over the block in a fixed order, then over units by the last unit.
@@ -229,9 +230,29 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
         }
         __syncwarp();
 #else
+#if defined(RF_GROUP_ROWS) && defined(RF_GROUP_SPLIT)
+        // RF_GROUP_ROWS rows a thread per iteration: all their loads (rf_group_ld) issued before
+        // any row is evaluated (rf_group_v), so a warp has that many rows' loads in flight
+#pragma unroll 1
+        for (long long r = r0 + tid; r < r1; r += (long long)RF_GROUP_ROWS * T) {
+            RfRowLd L[RF_GROUP_ROWS];
+#pragma unroll
+            for (int k = 0; k < RF_GROUP_ROWS; k++)
+                if (r + (long long)k * T < r1) rf_group_ld(P, r + (long long)k * T, L[k]);
+#pragma unroll
+            for (int k = 0; k < RF_GROUP_ROWS; k++) {
+                if (r + (long long)k * T >= r1) break;
+                RfVals V;
+                const int g = rf_group_v(P, r + (long long)k * T, L[k], V);
+                if (g >= 0) rf_slot_add(S, g, tid, V, df);
+            }
+        }
+#else
         // RF_GROUP_UNROLL 1 (a fragment with double-float sums): one row per iteration - the slot
-        // update is long, and unrolled rows cost registers the row's own latencies need (the
-        // 6-group group-by: 0.775 ms against 0.789 / 0.800 ms unrolled 2 / 4)
+        // update is long, and unrolled rows (whose loads the compiler does not move above the
+        // previous row's branches) cost registers the row's own latencies need (the 6-group
+        // group-by, its value loads after its filter: 0.775 ms against 0.789 / 0.800 ms unrolled
+        // 2 / 4)
 #if defined(RF_GROUP_UNROLL) && RF_GROUP_UNROLL == 1
 #pragma unroll 1
 #else
@@ -242,6 +263,7 @@ RF_DEV void rf_group_reduce(const RfParams& P, int unit, int nunits)
             int g = rf_group(P, r, V);
             if (g >= 0) rf_slot_add(S, g, tid, V, df);
         }
+#endif
 #endif
     }
     rf_slots_done(S, tid, df);
