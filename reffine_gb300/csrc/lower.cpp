@@ -1439,6 +1439,35 @@ private:
         return decl.str();
     }
 
+    // Loads of the driving row that a row's values read once it has passed its filter (text
+    // from position `from` on): each distinct load into one local, declared at `from`, so the
+    // compiler sees equal operands and computes a shared subexpression (price * (1 - disc) in
+    // two sums) once.  Same loads, same rounding: only repeated work goes.
+    static void hoist_value_loads(std::string& text, size_t from)
+    {
+        const std::string pat = "rf_ld<";
+        std::map<std::string, std::string> seen;
+        std::vector<std::string> order;
+        for (size_t pos = text.find(pat, from); pos != std::string::npos; pos = text.find(pat, pos + 1)) {
+            size_t e = text.find(", r)", pos);
+            if (e == std::string::npos) continue;
+            std::string call = text.substr(pos, e + 4 - pos);
+            if (call.find("P.t[") == std::string::npos || call.find('(', pat.size()) == std::string::npos) continue;
+            if (seen.count(call)) continue;
+            seen[call] = "lv" + std::to_string(order.size());
+            order.push_back(call);
+        }
+        if (order.empty()) return;
+        std::ostringstream decl;
+        for (auto& c : order) decl << "    const " << c.substr(pat.size(), c.find('>') - pat.size()) << " " << seen[c] << " = " << c << ";\n";
+        std::string tail = text.substr(from);
+        for (auto& c : order) {
+            size_t p;
+            while ((p = tail.find(c)) != std::string::npos) tail.replace(p, c.size(), seen[c]);
+        }
+        text = text.substr(0, from) + decl.str() + tail;
+    }
+
     // cost-ordered conjunction: cheap column predicates first, hash probes last
     // evaluation cost class of a condition: 1 per node, 20 per element or data read, 100 per
     // index probe (Locate)
@@ -2070,18 +2099,25 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         std::vector<std::string> dcls(E.decls.begin(), E.decls.end());
         std::vector<std::string*> pieces{&rowcond, &gbody};
         for (auto& dd : dcls) pieces.push_back(&dd);
-        // Every column of the driving row is read up front: the value columns with the filter's
-        // and the keys', and an index probe's key, so that a row waits on one round trip to
-        // memory before its probe and none after (the 6-group group-by: 0.776 -> 0.667 ms with
-        // its value columns read up front; the 200M-row join: 1.099 -> 1.074 ms with its probe
-        // key and value read up front)
+        // The driving row's columns are read up front: the filter's, the keys', an index
+        // probe's key, and - without a probe - the value columns, so that a row waits on one
+        // round trip to memory (the 6-group group-by: 0.776 -> 0.667 ms with its value columns
+        // read up front).  With a probe the values are read once the row has passed it: rows
+        // that miss then read no value sectors, and the scan pushes less of the probed index out
+        // of L2 (the 200M-row join: 1.099 ms with the probe key read inside the probe, 1.074 ms
+        // (5.88 GB read) with key and value up front, 1.050 ms (4.81 GB) with the key alone)
         bool probes = gbody.find("rf_locate") != std::string::npos || rowcond.find("rf_locate") != std::string::npos;
         std::string dtext;
         for (auto& dd : dcls) {
             probes = probes || dd.find("rf_locate") != std::string::npos;
             dtext += dd;
         }
-        std::string hoisted = hoist_row_loads(rowcond + gconds + dtext + gbody, pieces);
+        std::string hoisted = hoist_row_loads(rowcond + gconds + dtext + (probes ? std::string() : gbody), pieces);
+        if (probes) {
+            const std::string mk = "    if (g < 0) return -1;\n";
+            const size_t at = gbody.find(mk);
+            if (at != std::string::npos) hoist_value_loads(gbody, at + mk.size());
+        }
         std::ostringstream grp;
         // the row's loads as their own function (rf_group_ld into RfRowLd) and the rest
         // (rf_group_v), so that a kernel can issue the loads of two rows before it uses either
