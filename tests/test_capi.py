@@ -86,6 +86,68 @@ def test_only_full_row_grouped_scans_prefetch_the_next_tile():
     assert "RF_PREFETCH" not in engine.check(W.filter_sum_query(t.get_data_type()))
 
 
+def _row_sum_query(tbl_type, value_of):
+    # SUM over the rows of the group-by table of value_of(row's columns: flag_a, flag_b, qty,
+    # price, disc, tax, day)
+    vec = W._sym("lineitem", tbl_type)
+
+    def acc(s, v):
+        return W._add(s, value_of([W._get(v, i) for i in range(7)]))
+
+    red = W._red(W._subvec(vec, W._idx(0), W._len(vec, 1)), lambda: W._f64(0), acc)
+    red_sym = W._sym("red", red)
+    fn = W._func("rowsum", red_sym, [vec])
+    fn.tbl[red_sym] = red
+    return fn
+
+
+def test_one_minus_and_one_plus_products_lower_to_fused_forms():
+    # x*(1-y) and x*(1+y) over FP64 (either operand order) become rf_mul_1m / rf_mul_1p; other
+    # constants, the other subtraction order and plain products stay as written
+    tt = W.groupby_table(64).get_data_type()
+    cases = [(lambda c: W._mul(c[3], W._sub(W._f64(1), c[4])), "rf_mul_1m("),
+             (lambda c: W._mul(W._add(W._f64(1), c[5]), c[3]), "rf_mul_1p("),
+             (lambda c: W._mul(c[3], W._sub(W._f64(2), c[4])), None),
+             (lambda c: W._mul(c[3], W._sub(c[4], W._f64(1))), None),
+             (lambda c: W._mul(c[3], c[4]), None)]
+    for value_of, fused in cases:
+        src = engine.check(_row_sum_query(tt, value_of))
+        got = [f for f in ("rf_mul_1m(", "rf_mul_1p(") if f in src]
+        assert got == ([fused] if fused else []), (fused, got)
+    src = engine.check(W.groupby_query(tt))
+    assert "rf_mul_1p(rf_mul_1m(ld4, ld5), ld6)" in src
+
+
+def test_grouped_scan_loads_four_rows_before_evaluating_any():
+    # the group-by's row function is split into its loads (rf_group_ld: every column the row
+    # reads) and the rest (rf_group_v: no column load of its own), and the kernel takes four rows
+    # a thread per iteration
+    src = engine.check(W.groupby_query(W.groupby_table(64).get_data_type()))
+    assert "#define RF_GROUP_SPLIT 1" in src and "#define RF_GROUP_ROWS 4" in src
+    ld = src[src.index("RF_DEV void rf_group_ld("):]
+    ld = ld[:ld.index("\n}\n")]
+    cols = {int(c) for c in re.findall(r"rf_ld<\w+>\(P\.t\[0\]\.col\[(\d+)\]\.data, r\)", ld)}
+    assert cols == {1, 2, 3, 4, 5, 6, 7}
+    v = src[src.index("RF_DEV int rf_group_v("):]
+    v = v[:v.index("\n}\n")]
+    assert "rf_ld<" not in v
+
+
+def test_probe_kernel_reads_probe_key_first_and_value_after_the_probe():
+    # the join's row function loads the probe key with the row's other columns, ahead of the
+    # probe, and the summed value only once the row has passed it (and is not split for
+    # four-row steps: its rows come from the per-warp queue)
+    b, p = W.join_tables(64, 256)
+    src = engine.check(W.join_query(b.get_data_type(), p.get_data_type()))
+    g = src[src.index("RF_DEV int rf_group("):]
+    g = g[:g.index("\n}\n")]
+    key = g.index("rf_ld<int64_t>(P.t[1].col[1].data, r)")
+    assert key < g.index("rf_locate(")
+    assert "rf_locate(P.t[0].ix, (long long)(ld1))" in g
+    assert g.index("rf_ld<double>(P.t[1].col[2].data, r)") > g.index("if (g < 0) return -1;")
+    assert "RF_GROUP_SPLIT" not in src
+
+
 @pytest.mark.parametrize("vectorize", [False, True])
 def test_reference_reduce_queries_compile(vectorize):
     st2 = rq.students_table(2)
