@@ -2120,7 +2120,7 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
         }
         std::ostringstream grp;
         // the row's loads as their own function (rf_group_ld into RfRowLd) and the rest
-        // (rf_group_v), so that a kernel can issue the loads of two rows before it uses either
+        // (rf_group_v), so that a kernel can issue the loads of several rows before it uses any
         std::vector<std::array<std::string, 3>> hl;  // type, name, load call
         if (!probes) {
             std::istringstream in(hoisted);
