@@ -2149,11 +2149,15 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
             grp << gbody << "}\n\n";
             grp << "RF_DEV int rf_group(const RfParams& P, long long r, RfVals& V)\n{\n    RfRowLd L;\n"
                    "    rf_group_ld(P, r, L);\n    return rf_group_v(P, r, L, V);\n}\n\n#define RF_GROUP_SPLIT 1\n";
-            // four rows a thread per loop iteration, their loads issued together: more of each
-            // warp's row loads in flight (the 6-group group-by: 0.634 ms with one row, 0.584 /
-            // 0.598 / 0.563 / 0.581 / 0.564 / 0.607 ms with 2 / 3 / 4 / 5 / 6 / 8, each with the
-            // tuner's tiling)
-            grp << "#define RF_GROUP_ROWS 4\n";
+            // several rows a thread per loop iteration, their loads issued together: more of each
+            // warp's row loads in flight.  Four for a row of up to 12 register words (the 6-group
+            // group-by, 11: 0.634 ms with one row, 0.584 / 0.598 / 0.563 / 0.581 / 0.564 / 0.607
+            // ms with 2 / 3 / 4 / 5 / 6 / 8, each with the tuner's tiling); wider rows take two, or
+            // one past 32 words, so that the rows' values fit the registers (a group-by summing 12
+            // or 14 double columns spills 124 / 220 bytes with four rows, none with two)
+            int words = 0;
+            for (auto& h : hl) words += (h[0] == "double" || h[0] == "int64_t" || h[0] == "uint64_t") ? 2 : 1;
+            grp << "#define RF_GROUP_ROWS " << (words <= 12 ? 4 : words <= 32 ? 2 : 1) << "\n";
             grp << "\n";
         } else {
             grp << "RF_DEV int rf_group(const RfParams& P, long long r, RfVals& V)\n{\n";

@@ -133,6 +133,14 @@ def test_grouped_scan_loads_four_rows_before_evaluating_any():
     assert "rf_ld<" not in v
 
 
+def test_grouped_scan_takes_fewer_rows_per_step_for_wide_rows():
+    # four rows a step up to 12 register words of loaded columns, two up to 32, else one
+    from widequery import wide_groupby_query, wide_table
+    for ncol, rows in [(4, 4), (12, 2), (14, 2)]:
+        src = engine.check(wide_groupby_query(wide_table(64, ncol).get_data_type(), ncol))
+        assert "#define RF_GROUP_ROWS %d" % rows in src, ncol
+
+
 def test_probe_kernel_reads_probe_key_first_and_value_after_the_probe():
     # the join's row function loads the probe key with the row's other columns, ahead of the
     # probe, and the summed value only once the row has passed it (and is not split for

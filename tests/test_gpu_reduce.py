@@ -179,6 +179,18 @@ def test_groupby_fused_products_band_edges(eng):
     assert_same(got, loopgen.Query(fn)(t))
 
 
+@pytest.mark.parametrize("ncol", [4, 14])
+def test_wide_row_groupby_parity(eng, ncol):
+    # a grouped sum over 4 and 14 FP64 columns: four rows a thread per step for the narrow row,
+    # two for the wide one (its 30 register words of loaded columns)
+    from widequery import wide_groupby_query, wide_table
+    t = wide_table(700_001, ncol, seed=41)
+    fn = wide_groupby_query(t.get_data_type(), ncol)
+    plan = eng.compile(fn)
+    assert "#define RF_GROUP_ROWS %d" % (4 if ncol == 4 else 2) in plan.source()
+    assert_same(plan.run(eng.upload(t)), loopgen.Query(fn)(t))
+
+
 def test_groupby_mixed_signs_wide_exponents(eng):
     # grouped FP64 sums over addends of both signs spread over ~60 binades, with tiny, huge,
     # subnormal and signed-zero values at random rows
