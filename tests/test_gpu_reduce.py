@@ -187,7 +187,7 @@ def test_wide_row_groupby_parity(eng, ncol):
     t = wide_table(700_001, ncol, seed=41)
     fn = wide_groupby_query(t.get_data_type(), ncol)
     plan = eng.compile(fn)
-    assert "#define RF_GROUP_ROWS %d" % (4 if ncol == 4 else 2) in plan.source()
+    assert "#define RF_GROUP_ROWS %d" % (4 if ncol == 4 else 2) in plan.source
     assert_same(plan.run(eng.upload(t)), loopgen.Query(fn)(t))
 
 
