@@ -2154,7 +2154,8 @@ extern "C" __global__ void __launch_bounds__(256) rf_ixf_build(const __grid_cons
             // group-by, 11: 0.634 ms with one row, 0.584 / 0.598 / 0.563 / 0.581 / 0.564 / 0.607
             // ms with 2 / 3 / 4 / 5 / 6 / 8, each with the tuner's tiling); wider rows take two, or
             // one past 32 words, so that the rows' values fit the registers (a group-by summing 12
-            // or 14 double columns spills 124 / 220 bytes with four rows, none with two)
+            // or 14 double columns spills 124 / 220 bytes with four rows, none with two; the
+            // 14-column one on 4M rows: 0.204 ms with two rows a step, 0.215 ms with one)
             int words = 0;
             for (auto& h : hl) words += (h[0] == "double" || h[0] == "int64_t" || h[0] == "uint64_t") ? 2 : 1;
             grp << "#define RF_GROUP_ROWS " << (words <= 12 ? 4 : words <= 32 ? 2 : 1) << "\n";
