@@ -9,10 +9,12 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 import refqueries as rq
 from reffine_gb300 import _capi, engine, ir, workloads as W
+from reffine_gb300.table import Table
 from reffine_gb300.ir import _add, _f64, _func, _get, _i64, _idx, _len, _red, _subvec, _sym
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -139,6 +141,41 @@ def test_grouped_scan_takes_fewer_rows_per_step_for_wide_rows():
     for ncol, rows in [(4, 4), (12, 2), (14, 2)]:
         src = engine.check(wide_groupby_query(wide_table(64, ncol).get_data_type(), ncol))
         assert "#define RF_GROUP_ROWS %d" % rows in src, ncol
+
+
+def test_split_grouped_row_function_compiles_for_narrow_column_types():
+    # the grouped scan's split row function (RfRowLd members, rf_group_ld, rf_group_v) for int8
+    # keys and int16 / float32 / uint8 values: lowered and compiled for sm_103a
+    rng = np.random.default_rng(0)
+    n = 64
+    t = Table.from_arrays(2, {"key": np.arange(n, dtype=np.int64), "k": rng.integers(0, 2, n).astype(np.int8),
+                              "s16": rng.integers(-5, 5, n).astype(np.int16),
+                              "f32": rng.uniform(0, 1, n).astype(np.float32),
+                              "u8": rng.integers(0, 9, n).astype(np.uint8)}, name="mixed")
+    vec = ir._sym("m", t.get_data_type())
+
+    def acc(s, v):
+        k, s16, f32, u8 = (ir._get(v, i) for i in range(4))
+        out = []
+        for g in range(2):
+            c = ir._eq(k, ir._i8(g))
+            sg = ir._get(s, g)
+            out.append(ir._new([ir._sel(c, ir._add(ir._get(sg, 0), f32), ir._get(sg, 0)),
+                                ir._sel(c, ir._add(ir._get(sg, 1), ir._cast(ir._i64_t, s16)), ir._get(sg, 1)),
+                                ir._sel(c, ir._add(ir._get(sg, 2), ir._cast(ir._i64_t, u8)), ir._get(sg, 2))]))
+        return ir._new(out)
+
+    init = lambda: ir._new([ir._new([ir._f32(0), ir._i64(0), ir._i64(0)]) for _ in range(2)])
+    red = ir._red(ir._subvec(vec, ir._idx(0), ir._len(vec, 1)), init, acc)
+    red_sym = ir._sym("red", red)
+    fn = ir._func("mixed", red_sym, [vec])
+    fn.tbl[red_sym] = red
+    src = engine.check(fn)
+    assert "#define RF_GROUP_SPLIT 1" in src and "#define RF_GROUP_ROWS 4" in src
+    ld = src[src.index("struct RfRowLd {"):]
+    ld = ld[:ld.index("};")]
+    for ty in ("int8_t", "int16_t", "float", "uint8_t"):
+        assert "    %s ld" % ty in ld, ty
 
 
 def test_probe_kernel_reads_probe_key_first_and_value_after_the_probe():
